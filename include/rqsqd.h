@@ -1,0 +1,210 @@
+/*
+ * rqsqd.h -- C ABI of the GB300 (sm_103a) SQD hot path: the Pauli-sum matvec restricted to a
+ * sorted bitstring subspace, and the single-vector LOBPCG that drives it.
+ *
+ * Reference interfaces replaced (rqutils 0.2.0, pure JAX, no FFI of its own):
+ *   rq_subspace_build      uniquify_states / the sort inside get_xsource   rqutils/sqd.py:414-503
+ *   rq_xsource             get_xsource                                   rqutils/sqd.py:448-503
+ *   rq_diagonal            get_diagonal                                  rqutils/sqd.py:554-575
+ *   rq_conn_build          the cached X-source table (cache_level[0]==1) rqutils/sqd.py:318-326
+ *   rq_matvec              apply_h / apply_h_x_cached / apply_h_xz_cached rqutils/sqd.py:590-684
+ *   rq_fullspace_matvec    PauliSumXZ.matmul                             rqutils/paulis/symplectic.py:131-150
+ *   rq_lobpcg_solve        ground_locg / _ground_locg_callable            rqutils/ground_locg.py:128-377
+ *   rq_lobpcg_solve_cb     ground_locg with a user matvec or matrix      rqutils/ground_locg.py:154-179
+ *   rq_eigenpair_3x3       eigenpair_3x3                                 rqutils/ground_locg.py:438-471
+ *
+ * Conventions
+ *   - A basis state is a uint64 whose bit q is qubit q.  Subspaces are strictly increasing arrays
+ *     of such states (the reference's lexicographic order of packed bytes is the same order).
+ *   - A Hamiltonian is grouped by X signature: group j has X mask xmask[j] and terms
+ *     toff[j] <= k < toff[j+1] with Z mask zmask[k] and phased coefficient coef[2k] + i coef[2k+1]
+ *     (the coefficient times (-i)^popcount(x & z)).  Within a group the terms end at the first
+ *     zero coefficient, as in the reference's diagonal loop.
+ *   - (H v)[i] = sum_j sum_k c_jk (-1)^popcount(S[i] & z_jk) v[m],  S[m] = S[i] ^ x_j;
+ *     a term whose source S[i] ^ x_j is not in the subspace contributes nothing.
+ *   - Every pointer inside the structs below is a DEVICE pointer owned by the caller.  No entry
+ *     point allocates device memory; workspaces are sized by the *_size functions and passed in.
+ *   - Every call is ordered on the given stream (cudaStream_t passed as void*; NULL = legacy
+ *     default stream).  Calls that return a host-visible result synchronise that stream.
+ *   - Return value: RQ_OK (0) or an RQ_E* code; rq_last_error() gives a message (thread-local).
+ *   - Not thread-safe per workspace: concurrent calls must use distinct workspaces.
+ */
+#ifndef RQSQD_H
+#define RQSQD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* value types of vectors */
+#define RQ_F32  0   /* float                       */
+#define RQ_F64  1   /* double                      */
+#define RQ_C64  2   /* complex float  (re, im)     */
+#define RQ_C128 3   /* complex double (re, im)     */
+
+/* status codes */
+#define RQ_OK            0
+#define RQ_E_ARG         1   /* invalid argument / size                                   */
+#define RQ_E_CUDA        2   /* CUDA runtime error                                        */
+#define RQ_E_UNSORTED    3   /* subspace not strictly increasing                          */
+#define RQ_E_TABLE       4   /* hash table overflow (bounded probe or insert gave up)     */
+#define RQ_E_NONFINITE   5   /* a non-finite value appeared (LOBPCG breakdown)            */
+#define RQ_E_MAXITER     6   /* LOBPCG stopped at maxiter without meeting the tolerance   */
+#define RQ_E_RANGE       7   /* a size exceeds a fixed limit of the entry point           */
+
+/* lookup structures for S[i] ^ x membership */
+#define RQ_LOOKUP_HASH     0  /* bucketed open-addressing hash table (4 keys per 32-byte bucket) */
+#define RQ_LOOKUP_BSEARCH  1  /* shared-memory sampled binary search over the sorted states      */
+#define RQ_LOOKUP_IDENTITY 2  /* full space: S[i] = i, D = 2^n (PauliSumXZ.matmul)               */
+
+/* matvec modes (the reference's cache_level) */
+#define RQ_MODE_FREE 0   /* cache_level (0, *): lookups inside every matvec                        */
+#define RQ_MODE_CONN 1   /* cache_level (1, 0|1): connectivity cached, diagonals recomputed        */
+#define RQ_MODE_CSR  2   /* cache_level (*, 2): full CSR of matrix elements                        */
+
+#define RQ_FILTER_WORDS 133  /* 65 x 65 bitset of (popcount(s & fmask_a), popcount(s & fmask_b)) */
+
+typedef struct rq_subspace {
+    const uint64_t *states;  /* [D] strictly increasing                                   */
+    int64_t   D;             /* subspace dimension, 1 <= D < 2^31                          */
+    uint64_t *hkeys;         /* [4 << hbits] hash keys (RQ_LOOKUP_HASH)                    */
+    int32_t  *hvals;         /* [4 << hbits] row index of each key                         */
+    int32_t   hbits;         /* log2(number of buckets), from rq_subspace_sizes            */
+    int32_t   lookup;        /* RQ_LOOKUP_*                                                */
+    uint64_t  empty_key;     /* written by rq_subspace_build: a value not in states        */
+    uint64_t  fmask_a;       /* sector filter masks (0, 0 = filter off)                    */
+    uint64_t  fmask_b;
+    uint32_t *fbits;         /* [RQ_FILTER_WORDS], written by rq_subspace_build            */
+} rq_subspace_t;
+
+typedef struct rq_terms {
+    int32_t   J;             /* number of X groups                                         */
+    int32_t   K;             /* number of terms (sum of group sizes)                       */
+    int32_t   diag_group;    /* index of the group with x = 0, or -1                       */
+    int32_t   is_real;       /* 1 if every coefficient is real (real vectors allowed)      */
+    const uint64_t *xmask;   /* [J]                                                        */
+    const int32_t  *toff;    /* [J + 1]                                                    */
+    const uint64_t *zmask;   /* [K]                                                        */
+    const double   *coef;    /* [2K] interleaved (re, im)                                  */
+} rq_terms_t;
+
+typedef struct rq_operator {
+    rq_subspace_t sub;
+    rq_terms_t    terms;
+    int32_t       mode;      /* RQ_MODE_*                                                  */
+    int32_t       val_vtype; /* value type of `val` (RQ_MODE_CSR); a matvec of another type
+                                converts on load                                           */
+    const double *diag0;     /* [D] real diagonal of group diag_group, or NULL (computed)  */
+    const int64_t *rowptr;   /* [D + 1]  RQ_MODE_CONN / RQ_MODE_CSR                        */
+    const int32_t *col;      /* [nnz]    source row of each off-diagonal element           */
+    const int32_t *grp;      /* [nnz]    X group of each element (RQ_MODE_CONN)            */
+    const void    *val;      /* [nnz]    element values in the matvec's value type (CSR)   */
+    int64_t       nnz;
+} rq_operator_t;
+
+/* ---- sizing (host only) ---------------------------------------------------------------- */
+
+/* Hash-table bucket count exponent for D states at load factor <= 1/2 (4 slots per bucket). */
+int rq_subspace_sizes(int64_t D, int32_t *hbits);
+
+/* Bytes of scratch that rq_matvec / rq_conn_build / rq_dots need for their reductions/scans. */
+int rq_scratch_size(int64_t D, size_t *bytes);
+
+/* ---- subspace ---------------------------------------------------------------------------- */
+
+/* Validate strict increase, choose empty_key, fill the hash table and the sector filter.
+ * Synchronises the stream; returns RQ_E_UNSORTED when states is not strictly increasing. */
+int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream);
+
+/* get_xsource for J X masks: out[j * D + i] = m with S[m] = S[i] ^ xmask[j], else -1. */
+int rq_xsource(const rq_subspace_t *sub, const uint64_t *xmask, int32_t J, int32_t *out,
+               void *stream);
+
+/* get_diagonal: out[i] = sum_k c_k (-1)^popcount(S[i] & z_k), k < K, stopping at the first
+ * zero coefficient.  out is complex double [2D]. */
+int rq_diagonal(const uint64_t *states, int64_t D, const uint64_t *zmask, const double *coef,
+                int32_t K, double *out, void *stream);
+
+/* ---- connectivity cache ---------------------------------------------------------------- */
+
+/* Pass 1 (col == NULL): fill rowptr[D+1] and return nnz.  Pass 2: fill col / grp (and val in
+ * value type vtype when val != NULL) in row order, groups ascending within a row. */
+int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col, int32_t *grp,
+                  void *val, int32_t vtype, int64_t *nnz, void *scratch, void *stream);
+
+/* ---- matvec -------------------------------------------------------------------------------- */
+
+/* y = H x in value type vtype (RQ_F32 / RQ_F64 need terms.is_real).  x and y must not alias. */
+int rq_matvec(const rq_operator_t *op, int32_t vtype, const void *x, void *y, void *scratch,
+              void *stream);
+
+/* Full-space matvec (PauliSumXZ.matmul): D = 2^n, n <= 31, no subspace. */
+int rq_fullspace_matvec(const rq_terms_t *terms, int32_t n, int32_t vtype, const void *x,
+                        void *y, void *stream);
+
+/* ---- LOBPCG --------------------------------------------------------------------------------- */
+
+#define RQ_LOBPCG_REFERENCE 0   /* four matvecs per iteration, as ground_locg.py:288-341      */
+#define RQ_LOBPCG_FAST      1   /* one matvec per iteration (A x, A y carried by linearity)   */
+
+typedef struct rq_lobpcg_params {
+    int32_t maxiter;        /* per phase; reference default 1000                            */
+    int32_t variant;        /* RQ_LOBPCG_*                                                   */
+    int32_t vtype;          /* value type of the (final) phase: RQ_F64 or RQ_C128 (or 32-bit)*/
+    int32_t mixed;          /* 1: iterate first in the 32-bit type, then refine in vtype      */
+    double  tol;            /* <= 0: machine epsilon of vtype (reference default)            */
+    double  tol_dim;        /* vector length in the convergence test (<= 0: D)               */
+    double  switch_rel;     /* mixed: leave the 32-bit phase when |r| < switch_rel * |theta|  */
+    double  target_rel;     /* > 0: also stop when |r| <= target_rel * |theta| (FP64 residual) */
+    int32_t refresh;        /* FAST: recompute A x, A y every `refresh` iterations (0 = 32)  */
+    int32_t use_graph;      /* 1: run the loop as one CUDA graph with a device-side while    */
+    int32_t jacobi;         /* 1: precondition the residual with (diag(H) - theta)^-1        */
+    int32_t pad_;
+} rq_lobpcg_params_t;
+
+typedef struct rq_lobpcg_result {
+    double  eigval;         /* lowest Rayleigh-Ritz value                                      */
+    double  resnorm;        /* |A x - eigval x| in FP64 after the last iteration              */
+    double  axnorm;         /* |A x|                                                          */
+    int32_t niter;          /* loop iterations (all phases)                                   */
+    int32_t niter_lo;       /* iterations of the 32-bit phase                                 */
+    int32_t matvecs;        /* matvecs issued                                                 */
+    int32_t converged;      /* reference convergence test met                                 */
+    int32_t status;         /* RQ_OK / RQ_E_NONFINITE / RQ_E_MAXITER                          */
+    int32_t pad_;
+} rq_lobpcg_result_t;
+
+/* Workspace bytes for rq_lobpcg_solve on D rows. */
+int rq_lobpcg_workspace_size(int64_t D, const rq_lobpcg_params_t *prm, size_t *bytes);
+
+/* Lowest eigenpair of H from the initial vector x0 (value type prm->vtype, length D); the
+ * normalised eigenvector is written to x_out (same type).  Synchronises the stream. */
+int rq_lobpcg_solve(const rq_operator_t *op, const rq_lobpcg_params_t *prm, void *workspace,
+                    const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
+
+/* Matvec supplied by the caller: y = A x in value type vtype on `stream`; return 0 on success. */
+typedef int (*rq_matvec_fn)(void *ctx, int32_t vtype, const void *x, void *y, void *stream);
+
+/* rq_lobpcg_solve with the matvec supplied by the caller (ground_locg with a callable or a
+ * matrix, ground_locg.py:154-157).  Runs without graph capture, one iteration per launch batch. */
+int rq_lobpcg_solve_cb(int64_t D, rq_matvec_fn fn, void *ctx, const rq_lobpcg_params_t *prm,
+                       void *workspace, const void *x0, void *x_out, rq_lobpcg_result_t *res,
+                       void *stream);
+
+/* Lowest eigenpair of a Hermitian 3x3 (row-major complex double [18]) on the device, Cardano as
+ * ground_locg.py:438-471: writes lambda to out[0] and the eigenvector (complex) to out[2..7]. */
+int rq_eigenpair_3x3(const double *mat, double *out, void *stream);
+
+/* ---- diagnostics ------------------------------------------------------------------------- */
+
+const char *rq_last_error(void);
+int rq_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RQSQD_H */

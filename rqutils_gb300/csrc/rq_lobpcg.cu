@@ -1,0 +1,966 @@
+// Single-vector LOBPCG on the device (rqutils/ground_locg.py:182-471).
+//
+// Every step of the reference iteration is a fused pass over D-length vectors whose scalar
+// inputs (inner products, norms, the Ritz pair) live in a device-resident state block, so an
+// iteration never waits for the host.  Chunks of iterations are captured once into a CUDA graph
+// and relaunched; each kernel first reads the state's `active` flag and returns at once after
+// convergence, so a chunk may overshoot the last iteration at the cost of empty launches only.
+//
+// Reductions: FP64.  For 32-bit vectors each product is formed error-free in FP32 (p = a*b,
+// e = fma(a, b, -p)) and summed with TwoSum per thread before the FP64 grid reduction, so the
+// Gram entries carry FP64-level accuracy without FP64 arithmetic in the streaming loop.
+//
+// Variants: REFERENCE recomputes A x, A y and A p in every Rayleigh-Ritz step and A x' after the
+// update (four matvecs), as the reference does; FAST carries A x and A y by linearity (one matvec
+// per iteration) and recomputes them every `refresh` iterations and before accepting convergence.
+// Mixed precision runs a 32-bit phase first and continues in the 64-bit type from its x and y.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "rq_common.cuh"
+#include "rq_host.h"
+
+namespace rq {
+
+int matvec_dispatch(const rq_operator_t &op, int32_t vtype, const void *x, void *y, void *scratch,
+                    cudaStream_t st, const int *gate, const int *gate2);
+
+namespace {
+
+// ------------------------------------------------------------------------------------------
+// device state
+// ------------------------------------------------------------------------------------------
+enum Slot {
+    kIp0 = 0, kIp1 = 1, kVn = 2,                 // projection inner products, |v|^2
+    kG10 = 3, kG20 = 4, kG21 = 5, kG00 = 6, kG11 = 7, kG22 = 8,  // Gram entries
+    kSn = 9, kTn = 10, kUn = 11,                 // |s|^2, |t|^2, |u|^2
+    kAxn = 12, kRn = 13, kMisc = 14, kMisc2 = 15,
+    kSlots = 16
+};
+
+struct State {
+    double2 red[kSlots];
+    double2 kappa[3];
+    double theta;
+    double tol, tol_dim;
+    double switch_rel, target_rel;
+    double best_r;
+    double resnorm, axnorm;
+    int iter, maxiter;
+    int active, converged;
+    int status, phase_lo;
+    int stall, refresh;
+    int since_refresh, want_refresh;
+    int variant, matvecs;
+    int certify;  // FAST: the last convergence candidate must be confirmed by fresh products
+    int pad_[3];
+};
+
+// ------------------------------------------------------------------------------------------
+// error-free dot accumulation
+// ------------------------------------------------------------------------------------------
+template <typename R>
+struct DotAcc;
+
+template <>
+struct DotAcc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void prod(float a, float b) {
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);
+        float t, q;
+        two_sum(s, p, t, q);
+        s = t;
+        c += q + e;
+    }
+    __device__ __forceinline__ void nprod(float a, float b) { prod(-a, b); }
+    __device__ __forceinline__ double get() const { return (double)s + (double)c; }
+};
+
+template <>
+struct DotAcc<double> {
+    double s = 0.;
+    __device__ __forceinline__ void prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ void nprod(double a, double b) { s = fma(-a, b, s); }
+    __device__ __forceinline__ double get() const { return s; }
+};
+
+template <typename R>
+struct CDot {
+    DotAcc<R> re, im;
+    // conj(a) * b
+    __device__ __forceinline__ void add(cx<R> a, cx<R> b, bool cplx) {
+        re.prod(a.re, b.re);
+        if (cplx) {
+            re.prod(a.im, b.im);
+            im.prod(a.re, b.im);
+            im.nprod(a.im, b.re);
+        }
+    }
+    __device__ __forceinline__ double2 get() const { return make_double2(re.get(), im.get()); }
+};
+
+template <typename R>
+__device__ __forceinline__ cx<R> c_of(double2 v) { return {(R)v.x, (R)v.y}; }
+
+template <typename R>
+__device__ __forceinline__ cx<R> axpy(cx<R> a, cx<R> x, cx<R> y) {  // a*x + y
+    return {a.re * x.re - a.im * x.im + y.re, a.re * x.im + a.im * x.re + y.im};
+}
+
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+    const double den = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+#define GATE(st) \
+    if ((st)->active == 0) return;
+
+#define GRID_LOOP(i, D) \
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (D); i += (int64_t)gridDim.x * blockDim.x)
+
+// ------------------------------------------------------------------------------------------
+// vector kernels (one pass each)
+// ------------------------------------------------------------------------------------------
+
+// red[slot + k] = <a_k, b_k> for k < NP
+template <typename V, int NP>
+struct Pairs {
+    const V *a[NP];
+    const V *b[NP];
+};
+
+template <typename V, int NP>
+__global__ void __launch_bounds__(kThreads)
+k_dots(State *st, int64_t D, Pairs<V, NP> pr, int slot, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    CDot<R> acc[NP];
+    GRID_LOOP(i, D) {
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+            acc[k].add(VT<V>::ld(pr.a[k], i), VT<V>::ld(pr.b[k], i), VT<V>::kComplex);
+    }
+    double2 v[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) v[k] = acc[k].get();
+    grid_reduce<NP>(v, red, st->red + slot);
+}
+
+// out = v * scale where scale = 1 / sqrt(red[nslot].x) (1 when that is 0); optional <x,out>, <y,out>
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_normalize(State *st, int64_t D, const V *in, V *out, int nslot) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const double n = sqrt(st->red[nslot].x);
+    const R inv = (R)(n == 0. ? 1. : 1. / n);
+    GRID_LOOP(i, D) {
+        cx<R> v = VT<V>::ld(in, i);
+        VT<V>::st(out, i, {v.re * inv, v.im * inv});
+    }
+}
+
+// v <- v - x ip0 - y ip1 (ip from red[kIp0], red[kIp1]); red[kVn] = |v|^2
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_sub2_norm(State *st, int64_t D, const V *x, const V *y, V *v, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const cx<R> m0 = c_of<R>(make_double2(-st->red[kIp0].x, -st->red[kIp0].y));
+    const cx<R> m1 = c_of<R>(make_double2(-st->red[kIp1].x, -st->red[kIp1].y));
+    CDot<R> nn;
+    GRID_LOOP(i, D) {
+        cx<R> w = axpy(m0, VT<V>::ld(x, i), VT<V>::ld(v, i));
+        w = axpy(m1, VT<V>::ld(y, i), w);
+        VT<V>::st(v, i, w);
+        nn.add(w, w, VT<V>::kComplex);
+    }
+    double2 r[1] = {nn.get()};
+    grid_reduce<1>(r, red, st->red + kVn);
+}
+
+// v <- v / (|v| or 1); red[kIp0] = <x, v>, red[kIp1] = <y, v>
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_scale_dots2(State *st, int64_t D, const V *x, const V *y, V *v, int do_scale, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const double n = sqrt(st->red[kVn].x);
+    const R inv = (R)((!do_scale || n == 0.) ? 1. : 1. / n);
+    CDot<R> d0, d1;
+    GRID_LOOP(i, D) {
+        cx<R> w = VT<V>::ld(v, i);
+        w = {w.re * inv, w.im * inv};
+        if (do_scale) VT<V>::st(v, i, w);
+        d0.add(VT<V>::ld(x, i), w, VT<V>::kComplex);
+        d1.add(VT<V>::ld(y, i), w, VT<V>::kComplex);
+    }
+    double2 r[2] = {d0.get(), d1.get()};
+    grid_reduce<2>(r, red, st->red + kIp0);
+}
+
+// p = v if |v| >= 0.99 else 0 (ground_locg.py:421)
+template <typename V>
+__global__ void __launch_bounds__(kThreads) k_mask(State *st, int64_t D, const V *v, V *p) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const R m = (R)(sqrt(st->red[kVn].x) >= 0.99 ? 1. : 0.);
+    GRID_LOOP(i, D) {
+        cx<R> w = VT<V>::ld(v, i);
+        VT<V>::st(p, i, {w.re * m, w.im * m});
+    }
+}
+
+// Gram entries of (x, y, p): <y,Ax> <p,Ax> <p,Ay> <x,Ax> <y,Ay> <p,Ap>
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_gram3(State *st, int64_t D, const V *x, const V *y, const V *p, const V *ax, const V *ay,
+        const V *ap, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    CDot<R> g[6];
+    const bool c = VT<V>::kComplex;
+    GRID_LOOP(i, D) {
+        const cx<R> xi = VT<V>::ld(x, i), yi = VT<V>::ld(y, i), pi = VT<V>::ld(p, i);
+        const cx<R> axi = VT<V>::ld(ax, i), ayi = VT<V>::ld(ay, i), api = VT<V>::ld(ap, i);
+        g[0].add(yi, axi, c);
+        g[1].add(pi, axi, c);
+        g[2].add(pi, ayi, c);
+        g[3].add(xi, axi, c);
+        g[4].add(yi, ayi, c);
+        g[5].add(pi, api, c);
+    }
+    double2 r[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r[k] = g[k].get();
+    grid_reduce<6>(r, red, st->red + kG10);
+}
+
+// Gram entries of (x, p) for the first Rayleigh-Ritz step: <p,Ax> <x,Ax> <p,Ap>
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_gram2(State *st, int64_t D, const V *x, const V *p, const V *ax, const V *ap, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    CDot<R> g[3];
+    const bool c = VT<V>::kComplex;
+    GRID_LOOP(i, D) {
+        const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
+        const cx<R> axi = VT<V>::ld(ax, i), api = VT<V>::ld(ap, i);
+        g[0].add(pi, axi, c);
+        g[1].add(xi, axi, c);
+        g[2].add(pi, api, c);
+    }
+    double2 r[3] = {g[0].get(), g[1].get(), g[2].get()};
+    grid_reduce<3>(r, red, st->red + kG10);
+}
+
+// s = k1 y + k2 p: red[kSn] = |s|^2
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_upd_s(State *st, int64_t D, const V *y, const V *p, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const cx<R> k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
+    CDot<R> nn;
+    GRID_LOOP(i, D) {
+        const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
+        nn.add(s, s, VT<V>::kComplex);
+    }
+    double2 r[1] = {nn.get()};
+    grid_reduce<1>(r, red, st->red + kSn);
+}
+
+// t = s (k0/|s|) - x |s|, u = k0 x + s: red[kTn] = |t|^2, red[kUn] = |u|^2
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_upd_tu(State *st, int64_t D, const V *x, const V *y, const V *p, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const double ns = sqrt(st->red[kSn].x);
+    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
+    const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
+    const cx<R> mns = {(R)(-ns), (R)0};
+    CDot<R> tn, un;
+    GRID_LOOP(i, D) {
+        const cx<R> xi = VT<V>::ld(x, i);
+        const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
+        const cx<R> t = axpy(mns, xi, cmul(k0s, s));
+        const cx<R> u = axpy(k0, xi, s);
+        tn.add(t, t, VT<V>::kComplex);
+        un.add(u, u, VT<V>::kComplex);
+    }
+    double2 r[2] = {tn.get(), un.get()};
+    grid_reduce<2>(r, red, st->red + kTn);
+}
+
+// x <- u / |u|, y <- t / |t|; FAST also carries A x, A y by the same combinations.
+template <typename V, bool CARRY>
+__global__ void __launch_bounds__(kThreads)
+k_upd_xy(State *st, int64_t D, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const double ns = sqrt(st->red[kSn].x);
+    const double it = 1. / sqrt(st->red[kTn].x), iu = 1. / sqrt(st->red[kUn].x);
+    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
+    const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
+    const cx<R> mns = {(R)(-ns), (R)0};
+    const R rit = (R)it, riu = (R)iu;
+    GRID_LOOP(i, D) {
+        const cx<R> xi = VT<V>::ld(x, i);
+        const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
+        const cx<R> t = axpy(mns, xi, cmul(k0s, s));
+        const cx<R> u = axpy(k0, xi, s);
+        VT<V>::st(x, i, {u.re * riu, u.im * riu});
+        VT<V>::st(y, i, {t.re * rit, t.im * rit});
+        if (CARRY) {
+            const cx<R> axi = VT<V>::ld(ax, i);
+            const cx<R> as = axpy(k2, VT<V>::ld(ap, i), cmul(k1, VT<V>::ld(ay, i)));
+            const cx<R> at = axpy(mns, axi, cmul(k0s, as));
+            const cx<R> au = axpy(k0, axi, as);
+            VT<V>::st(ax, i, {au.re * riu, au.im * riu});
+            VT<V>::st(ay, i, {at.re * rit, at.im * rit});
+        }
+    }
+}
+
+// iteration 1 update (ground_locg.py:278-281): t = p k0 - x k1, u = x k0 + p k1 -> norms
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_upd2_norms(State *st, int64_t D, const V *x, const V *p, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]);
+    const cx<R> mk1 = {-k1.re, -k1.im};
+    CDot<R> tn, un;
+    GRID_LOOP(i, D) {
+        const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
+        const cx<R> t = axpy(mk1, xi, cmul(k0, pi));
+        const cx<R> u = axpy(k1, pi, cmul(k0, xi));
+        tn.add(t, t, VT<V>::kComplex);
+        un.add(u, u, VT<V>::kComplex);
+    }
+    double2 r[2] = {tn.get(), un.get()};
+    grid_reduce<2>(r, red, st->red + kTn);
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_upd2_xy(State *st, int64_t D, V *x, V *y, const V *p) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]);
+    const cx<R> mk1 = {-k1.re, -k1.im};
+    const R rit = (R)(1. / sqrt(st->red[kTn].x)), riu = (R)(1. / sqrt(st->red[kUn].x));
+    GRID_LOOP(i, D) {
+        const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
+        const cx<R> t = axpy(mk1, xi, cmul(k0, pi));
+        const cx<R> u = axpy(k1, pi, cmul(k0, xi));
+        VT<V>::st(x, i, {u.re * riu, u.im * riu});
+        VT<V>::st(y, i, {t.re * rit, t.im * rit});
+    }
+}
+
+// r = Ax - theta x; red[kAxn] = |Ax|^2, red[kRn] = |r|^2.  theta from st->theta, or from
+// Re red[kMisc] (iteration 0: rho = Re <x, Ax>) when use_rho.
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_resid(State *st, int64_t D, const V *ax, const V *x, V *r, int use_rho, void *red) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const double th = use_rho ? st->red[kMisc].x : st->theta;
+    const cx<R> mth = {(R)(-th), (R)0};
+    CDot<R> an, rn;
+    GRID_LOOP(i, D) {
+        const cx<R> a = VT<V>::ld(ax, i);
+        const cx<R> w = axpy(mth, VT<V>::ld(x, i), a);
+        VT<V>::st(r, i, w);
+        an.add(a, a, VT<V>::kComplex);
+        rn.add(w, w, VT<V>::kComplex);
+    }
+    double2 out[2] = {an.get(), rn.get()};
+    grid_reduce<2>(out, red, st->red + kAxn);
+}
+
+// w = r / (d - theta), |d - theta| floored at 1e-8 (1 + |theta|): the Jacobi preconditioner.
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_jacobi(State *st, int64_t D, const double *diag, const V *r, V *w) {
+    GATE(st);
+    using R = typename VT<V>::R;
+    const double th = st->theta;
+    const double floor_ = 1e-8 * (1. + fabs(th));
+    GRID_LOOP(i, D) {
+        double den = diag[i] - th;
+        if (fabs(den) < floor_) den = den < 0 ? -floor_ : floor_;
+        const R f = (R)(1. / den);
+        const cx<R> v = VT<V>::ld(r, i);
+        VT<V>::st(w, i, {v.re * f, v.im * f});
+    }
+}
+
+template <typename VS, typename VD>
+__global__ void __launch_bounds__(kThreads) k_convert(int64_t D, const VS *a, VD *b) {
+    using RS = typename VT<VS>::R;
+    using RD = typename VT<VD>::R;
+    GRID_LOOP(i, D) {
+        const cx<RS> v = VT<VS>::ld(a, i);
+        VT<VD>::st(b, i, {(RD)v.re, (RD)v.im});
+    }
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kThreads) k_copy(State *st, int64_t D, const V *a, V *b) {
+    GATE(st);
+    GRID_LOOP(i, D) b[i] = a[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// scalar kernels (one thread)
+// ------------------------------------------------------------------------------------------
+
+// Lowest eigenpair of a Hermitian 3x3 given by its strict lower triangle (m10, m20, m21) and its
+// diagonal (complex values, real part used as in ground_locg.py:446); Cardano (Kopp 2008).
+__device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2 m11, double2 m22,
+                     double &lam, double2 (&v)[3]) {
+    const double d0 = m00.x, d1 = m11.x, d2 = m22.x;
+    const double a10 = m10.x * m10.x + m10.y * m10.y;
+    const double a20 = m20.x * m20.x + m20.y * m20.y;
+    const double a21 = m21.x * m21.x + m21.y * m21.y;
+    const double c2 = -(d0 + d1 + d2);
+    const double c1 = (d0 * d2 + d1 * d0 + d2 * d1) - (a10 + a20 + a21);
+    double c0 = d0 * a21 + d1 * a20 + d2 * a10;
+    c0 -= d0 * d1 * d2;
+    // Re(m02 m10 m21) with m02 = conj(m20)
+    const double2 m02 = make_double2(m20.x, -m20.y);
+    const double2 t = make_double2(m02.x * m10.x - m02.y * m10.y, m02.x * m10.y + m02.y * m10.x);
+    c0 -= 2. * (t.x * m21.x - t.y * m21.y);
+    const double p = c2 * c2 - 3. * c1;
+    const double q = -13.5 * c0 - c2 * c2 * c2 + 4.5 * c2 * c1;
+    const double phi = atan2(sqrt(27. * (0.25 * c1 * c1 * (p - c1) + c0 * (q + 6.75 * c0))), q) / 3.;
+    const double cp = cos(phi), sp = sin(phi), s3 = sqrt(3.);
+    double xmin = 2. * cp;
+    xmin = fmin(xmin, -cp - s3 * sp);
+    xmin = fmin(xmin, -cp + s3 * sp);
+    if (isnan(cp) || isnan(sp)) xmin = NAN;  // jnp.min propagates NaN
+    lam = sqrt(p) / 3. * xmin - c2 / 3.;
+    // columns 1 and 2 of (A - lambda I): a = (m01, m11 - l, m21), b = (m02, m12, m22 - l)
+    const double2 a0 = make_double2(m10.x, -m10.y), a1 = make_double2(m11.x - lam, m11.y), a2 = m21;
+    const double2 b0 = m02, b1 = make_double2(m21.x, -m21.y), b2 = make_double2(m22.x - lam, m22.y);
+    auto mul = [](double2 u, double2 w) {
+        return make_double2(u.x * w.x - u.y * w.y, u.x * w.y + u.y * w.x);
+    };
+    auto sub = [](double2 u, double2 w) { return make_double2(u.x - w.x, u.y - w.y); };
+    double2 c[3] = {sub(mul(a1, b2), mul(a2, b1)), sub(mul(a2, b0), mul(a0, b2)),
+                    sub(mul(a0, b1), mul(a1, b0))};
+    double nrm = 0.;
+    for (int k = 0; k < 3; ++k) {
+        c[k].y = -c[k].y;  // conjugate
+        nrm += c[k].x * c[k].x + c[k].y * c[k].y;
+    }
+    nrm = sqrt(nrm);
+    for (int k = 0; k < 3; ++k) v[k] = make_double2(c[k].x / nrm, c[k].y / nrm);
+}
+
+__global__ void k_rr3(State *st) {
+    GATE(st);
+    double lam;
+    double2 v[3];
+    eig3(st->red[kG10], st->red[kG20], st->red[kG21], st->red[kG00], st->red[kG11], st->red[kG22],
+         lam, v);
+    st->theta = lam;
+    for (int k = 0; k < 3; ++k) st->kappa[k] = v[k];
+}
+
+// eigenpair_2x2 (ground_locg.py:424-435) of [[g00, conj(g10)], [g10, g11]]
+__global__ void k_rr2(State *st) {
+    GATE(st);
+    // k_gram2 wrote <p,Ax>, <x,Ax>, <p,Ap> to three consecutive slots from kG10
+    const double2 m10 = st->red[kG10];
+    const double d0 = st->red[kG10 + 1].x;  // <x, Ax>
+    const double d1 = st->red[kG10 + 2].x;  // <p, Ap>
+    const double det = d0 * d1 - (m10.x * m10.x + m10.y * m10.y);
+    const double tr = d0 + d1;
+    const double lam = (tr - sqrt(tr * tr - 4. * det)) * 0.5;
+    const double2 num = make_double2(d1 - lam + m10.x, -m10.y);
+    const double2 den = make_double2(d0 - lam + m10.x, m10.y);
+    double2 v0 = cdiv(num, den);
+    const double n = sqrt(v0.x * v0.x + v0.y * v0.y + 1.);
+    st->theta = lam;
+    st->kappa[0] = make_double2(v0.x / n, v0.y / n);
+    st->kappa[1] = make_double2(-1. / n, 0.);
+    st->kappa[2] = make_double2(0., 0.);
+}
+
+// iteration 0: rho = Re <x, Ax> into red[kMisc] (already there from k_dots); nothing else.
+
+// Convergence test of ground_locg.py:329-334 and phase bookkeeping.
+__global__ void k_check(State *st) {
+    GATE(st);
+    const double rn = sqrt(st->red[kRn].x);
+    const double an = sqrt(st->red[kAxn].x);
+    const double th = st->theta;
+    st->resnorm = rn;
+    st->axnorm = an;
+    st->iter += 1;
+    ++st->since_refresh;
+    bool conv = rn < st->tol * ((an - th) * st->tol_dim * 10.);
+    if (st->target_rel > 0. && rn <= st->target_rel * fabs(th)) conv = true;
+    if (!isfinite(rn) || !isfinite(th)) st->status = RQ_E_NONFINITE;
+    if (st->phase_lo) {
+        // 32-bit phase: hand over once the residual is small or stops improving
+        if (rn < st->switch_rel * fabs(th)) conv = true;
+        if (rn < 0.7 * st->best_r) {
+            st->best_r = rn;
+            st->stall = 0;
+        } else if (++st->stall >= 30) {
+            conv = true;
+        }
+    }
+    if (st->variant == RQ_LOBPCG_FAST) {
+        // carried products: confirm with fresh A x, A y before accepting
+        if (conv && !st->certify) {
+            st->want_refresh = 1;
+            st->certify = 1;
+            conv = false;
+        } else if (conv) {
+            st->certify = 0;
+        } else {
+            st->certify = 0;
+            st->want_refresh = (st->since_refresh >= st->refresh) ? 1 : 0;
+        }
+    }
+    st->converged = conv ? 1 : 0;
+    if (conv || st->iter >= st->maxiter) st->active = 0;
+}
+
+// FAST: a refresh starts -- reset the counter (runs only when want_refresh is set)
+__global__ void k_refresh_mark(State *st) {
+    GATE(st);
+    if (st->want_refresh) {
+        st->since_refresh = 0;
+        st->matvecs += 2;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// host driver
+// ------------------------------------------------------------------------------------------
+constexpr int kChunk = 8;  // iterations per captured graph (1 with a matvec callback)
+
+struct Layout {
+    size_t state, red, err, vec_lo, vec_hi, total;
+    int64_t D;
+    size_t lo_bytes, hi_bytes;
+};
+
+int lo_type(int32_t hi) {
+    switch (hi) {
+        case RQ_F64: return RQ_F32;
+        case RQ_C128: return RQ_C64;
+        default: return hi;
+    }
+}
+
+Layout layout(int64_t D, const rq_lobpcg_params_t &p) {
+    Layout L{};
+    L.D = D;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        size_t o = off;
+        off += (b + 255) & ~size_t(255);
+        return o;
+    };
+    L.state = take(sizeof(State));
+    L.err = take(16);
+    L.red = take(reduce_scratch_bytes());
+    L.hi_bytes = (size_t)D * vtype_size(p.vtype);
+    L.lo_bytes = (size_t)D * vtype_size(lo_type(p.vtype));
+    L.vec_hi = take(8 * ((L.hi_bytes + 255) & ~size_t(255)));
+    L.vec_lo = p.mixed ? take(8 * ((L.lo_bytes + 255) & ~size_t(255))) : 0;
+    L.total = off;
+    return L;
+}
+
+int grid_vec(int64_t D) {
+    int64_t g = (D + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)sm_count() * 4;
+    if (g > cap) g = cap;
+    if (g > kMaxReduceBlocks) g = kMaxReduceBlocks;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// Vectors of one phase: x, y, r, p, Ax, Ay, Ap, w.
+template <typename V>
+struct Vecs {
+    V *x, *y, *r, *p, *ax, *ay, *ap, *w;
+};
+
+template <typename V>
+Vecs<V> carve_vecs(char *base, size_t bytes) {
+    const size_t s = (bytes + 255) & ~size_t(255);
+    Vecs<V> v;
+    V **ptr[8] = {&v.x, &v.y, &v.r, &v.p, &v.ax, &v.ay, &v.ap, &v.w};
+    for (int k = 0; k < 8; ++k) *ptr[k] = reinterpret_cast<V *>(base + k * s);
+    return v;
+}
+
+template <typename V>
+struct Phase {
+    rq_matvec_fn fn;  // caller-supplied matvec, or null for the operator's own kernels
+    void *ctx;
+    const rq_operator_t *op;
+    int32_t vtype;
+    State *st;
+    void *red;
+    void *mvscratch;  // scratch for the matvec (its error flag)
+    Vecs<V> v;
+    int64_t D;
+    int grid;
+    bool jacobi;
+    const double *diag;
+
+    int matvec(const V *in, V *out, cudaStream_t s, const int *gate2 = nullptr) {
+        ++issued;
+        if (fn) {
+            if (gate2) return RQ_OK;  // FAST refreshes need the gate; callbacks use REFERENCE
+            const int rc = fn(ctx, vtype, in, out, s);
+            return rc == 0 ? RQ_OK : fail(RQ_E_ARG, "rq_lobpcg_solve_cb: the matvec callback failed");
+        }
+        return matvec_dispatch(*op, vtype, in, out, mvscratch, s, &st->active, gate2);
+    }
+    int issued = 0;
+
+    // project_out((x, y), src) -> p  (ground_locg.py:380-421); src is overwritten
+    void project(V *src, cudaStream_t s) {
+        Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
+        k_dots<V, 2><<<grid, kThreads, 0, s>>>(st, D, pr, kIp0, red);
+        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
+        k_scale_dots2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, 1, red);
+        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
+        k_scale_dots2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, 1, red);
+        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
+        k_scale_dots2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, 0, red);
+        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
+        k_mask<V><<<grid, kThreads, 0, s>>>(st, D, src, v.p);
+    }
+
+    // one loop iteration (ground_locg.py:288-341)
+    int iteration(int variant, cudaStream_t s) {
+        V *src = v.r;
+        if (jacobi) {
+            k_jacobi<V><<<grid, kThreads, 0, s>>>(st, D, diag, v.r, v.w);
+            src = v.w;
+        }
+        project(src, s);
+        if (variant == RQ_LOBPCG_REFERENCE) {
+            RQ_TRY(matvec(v.x, v.ax, s));
+            RQ_TRY(matvec(v.y, v.ay, s));
+        }
+        RQ_TRY(matvec(v.p, v.ap, s));
+        k_gram3<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, v.ax, v.ay, v.ap, red);
+        k_rr3<<<1, 1, 0, s>>>(st);
+        k_upd_s<V><<<grid, kThreads, 0, s>>>(st, D, v.y, v.p, red);
+        k_upd_tu<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, red);
+        if (variant == RQ_LOBPCG_REFERENCE) {
+            k_upd_xy<V, false><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, nullptr, nullptr, nullptr);
+            RQ_TRY(matvec(v.x, v.ax, s));
+        } else {
+            k_upd_xy<V, true><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+            // periodic / certifying refresh of the carried products
+            RQ_TRY(matvec(v.x, v.ax, s, &st->want_refresh));
+            RQ_TRY(matvec(v.y, v.ay, s, &st->want_refresh));
+            k_refresh_mark<<<1, 1, 0, s>>>(st);
+        }
+        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
+        k_check<<<1, 1, 0, s>>>(st);
+        RQ_CUDA(cudaGetLastError());
+        return RQ_OK;
+    }
+
+    // iterations 0 and 1 from v.x (unnormalised), ground_locg.py:264-286, 346
+    int start(cudaStream_t s) {
+        Pairs<V, 1> nx{{v.x}, {v.x}};
+        k_dots<V, 1><<<grid, kThreads, 0, s>>>(st, D, nx, kMisc2, red);
+        k_normalize<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.x, kMisc2);
+        RQ_TRY(matvec(v.x, v.ax, s));
+        Pairs<V, 1> rho{{v.x}, {v.ax}};
+        k_dots<V, 1><<<grid, kThreads, 0, s>>>(st, D, rho, kMisc, red);
+        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 1, red);
+        // iteration 1: p = r / |r|
+        k_normalize<V><<<grid, kThreads, 0, s>>>(st, D, v.r, v.p, kRn);
+        RQ_TRY(matvec(v.x, v.ax, s));
+        RQ_TRY(matvec(v.p, v.ap, s));
+        k_gram2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.p, v.ax, v.ap, red);
+        k_rr2<<<1, 1, 0, s>>>(st);
+        k_upd2_norms<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.p, red);
+        k_upd2_xy<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p);
+        RQ_TRY(matvec(v.x, v.ax, s));
+        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
+        RQ_CUDA(cudaGetLastError());
+        return RQ_OK;
+    }
+
+    // continuation from x, y of another phase (already converted into v.x, v.y): fresh A x, r
+    int resume(int variant, cudaStream_t s) {
+        RQ_TRY(matvec(v.x, v.ax, s));
+        if (variant == RQ_LOBPCG_FAST) RQ_TRY(matvec(v.y, v.ay, s));
+        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
+        RQ_CUDA(cudaGetLastError());
+        return RQ_OK;
+    }
+
+    // FAST: A x and A y recomputed (gated by want_refresh through a copy of the flag)
+    int refresh(cudaStream_t s) {
+        RQ_TRY(matvec(v.x, v.ax, s));
+        RQ_TRY(matvec(v.y, v.ay, s));
+        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
+        RQ_CUDA(cudaGetLastError());
+        return RQ_OK;
+    }
+};
+
+struct HostState {
+    int iter, active, converged, status;
+};
+
+int read_flags(State *st, HostState &h, cudaStream_t s) {
+    int buf[4];
+    RQ_CUDA(cudaMemcpyAsync(buf, &st->iter, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaMemcpyAsync(buf + 1, &st->active, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaMemcpyAsync(buf + 3, &st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaStreamSynchronize(s));
+    h.iter = buf[0];
+    h.active = buf[1];
+    h.converged = buf[2];
+    h.status = buf[3];
+    return RQ_OK;
+}
+
+// Run iterations until the state goes inactive.  With use_graph the chunk is captured once and
+// relaunched; otherwise launched eagerly.
+template <typename V>
+int run_loop(Phase<V> &ph, int variant, bool use_graph, cudaStream_t s) {
+    HostState h{};
+    const int chunk = ph.fn ? 1 : kChunk;
+    auto enqueue_chunk = [&](cudaStream_t cs) -> int {
+        for (int k = 0; k < chunk; ++k) RQ_TRY(ph.iteration(variant, cs));
+        return RQ_OK;
+    };
+    if (!use_graph) {
+        while (true) {
+            RQ_TRY(enqueue_chunk(s));
+            RQ_TRY(read_flags(ph.st, h, s));
+            if (!h.active) break;
+        }
+        return RQ_OK;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    RQ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_chunk(s);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc != RQ_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    RQ_CUDA(e);
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    RQ_CUDA(e);
+    while (true) {
+        e = cudaGraphLaunch(exec, s);
+        if (e != cudaSuccess) break;
+        rc = read_flags(ph.st, h, s);
+        if (rc != RQ_OK || !h.active) break;
+    }
+    cudaGraphExecDestroy(exec);
+    RQ_CUDA(e);
+    return rc;
+}
+
+template <typename V>
+int init_state(State *st, const rq_lobpcg_params_t &p, double tol, double tol_dim, bool lo,
+               int maxiter, cudaStream_t s) {
+    State h{};
+    h.tol = tol;
+    h.tol_dim = tol_dim;
+    h.switch_rel = p.switch_rel > 0 ? p.switch_rel : 1e-5;
+    h.target_rel = lo ? 0. : p.target_rel;
+    h.best_r = INFINITY;
+    h.maxiter = maxiter;
+    h.active = 1;
+    h.phase_lo = lo ? 1 : 0;
+    h.refresh = p.refresh > 0 ? p.refresh : 32;
+    h.variant = p.variant;
+    RQ_CUDA(cudaMemcpyAsync(st, &h, sizeof(State), cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaStreamSynchronize(s));  // h is a stack object
+    return RQ_OK;
+}
+
+template <typename VLO, typename VHI>
+int solve(const rq_operator_t &op, rq_matvec_fn fn, void *ctx, const rq_lobpcg_params_t &p,
+          char *ws, const void *x0, void *xout, rq_lobpcg_result_t *res, cudaStream_t s) {
+    const int64_t D = op.sub.D;
+    const Layout L = layout(D, p);
+    State *st = reinterpret_cast<State *>(ws + L.state);
+    void *red = ws + L.red;
+    // the matvec's scratch: its error flag sits 16 bytes into the area we hand it
+    void *mvscratch = ws + L.err - kScratchErr;
+    RQ_CUDA(cudaMemsetAsync(ws + L.err, 0, 16, s));
+    RQ_CUDA(cudaMemsetAsync(red, 0, 16, s));
+    const double tol_dim = p.tol_dim > 0 ? p.tol_dim : (double)D;
+    const bool jac = p.jacobi != 0 && op.diag0 != nullptr;
+    const int grid = grid_vec(D);
+    const int hi_type = p.vtype;
+    const bool cplx = (hi_type == RQ_C64 || hi_type == RQ_C128);
+    const double eps_hi = (hi_type == RQ_F32 || hi_type == RQ_C64) ? 1.1920928955078125e-07
+                                                                   : 2.220446049250313e-16;
+    const double tol = p.tol > 0 ? p.tol : eps_hi;
+    (void)cplx;
+
+    Phase<VHI> hi{fn, ctx, &op, hi_type, st, red, mvscratch,
+                  carve_vecs<VHI>(ws + L.vec_hi, L.hi_bytes), D, grid, jac, op.diag0};
+    int niter_lo = 0, matvec_lo = 0;
+    if (p.mixed && lo_type(hi_type) != hi_type) {
+        Phase<VLO> lo{fn, ctx, &op, lo_type(hi_type), st, red, mvscratch,
+                      carve_vecs<VLO>(ws + L.vec_lo, L.lo_bytes), D, grid, jac, op.diag0};
+        RQ_TRY(init_state<VLO>(st, p, 1.1920928955078125e-07, tol_dim, true, p.maxiter, s));
+        k_convert<VHI, VLO><<<grid, kThreads, 0, s>>>(D, static_cast<const VHI *>(x0), lo.v.x);
+        RQ_TRY(lo.start(s));
+        if (p.maxiter > 0) RQ_TRY(run_loop<VLO>(lo, p.variant, p.use_graph != 0, s));
+        HostState h{};
+        RQ_TRY(read_flags(st, h, s));
+        niter_lo = h.iter;
+        // continue in the 64-bit type from x and y
+        k_convert<VLO, VHI><<<grid, kThreads, 0, s>>>(D, lo.v.x, hi.v.x);
+        k_convert<VLO, VHI><<<grid, kThreads, 0, s>>>(D, lo.v.y, hi.v.y);
+        double theta_lo = 0.;
+        RQ_CUDA(cudaMemcpyAsync(&theta_lo, &st->theta, sizeof(double), cudaMemcpyDeviceToHost, s));
+        RQ_CUDA(cudaStreamSynchronize(s));
+        RQ_TRY(init_state<VHI>(st, p, tol, tol_dim, false, p.maxiter, s));
+        RQ_CUDA(cudaMemcpyAsync(&st->theta, &theta_lo, sizeof(double), cudaMemcpyHostToDevice, s));
+        RQ_TRY(hi.resume(p.variant, s));
+        RQ_CUDA(cudaStreamSynchronize(s));  // theta_lo is a stack value
+    } else {
+        RQ_TRY(init_state<VHI>(st, p, tol, tol_dim, false, p.maxiter, s));
+        RQ_CUDA(cudaMemcpyAsync(hi.v.x, x0, L.hi_bytes, cudaMemcpyDeviceToDevice, s));
+        RQ_TRY(hi.start(s));
+    }
+    if (p.maxiter > 0) RQ_TRY(run_loop<VHI>(hi, p.variant, p.use_graph != 0, s));
+    State h{};
+    int mv_err = 0;
+    RQ_CUDA(cudaMemcpyAsync(&h, st, sizeof(State), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaMemcpyAsync(&mv_err, ws + L.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaMemcpyAsync(xout, hi.v.x, L.hi_bytes, cudaMemcpyDeviceToDevice, s));
+    RQ_CUDA(cudaStreamSynchronize(s));
+    if (mv_err) return fail(mv_err, "rq_lobpcg_solve: matvec reported an error");
+    res->eigval = p.maxiter > 0 ? h.theta : 0.;  // the loop's initial theta (ground_locg.py:358)
+    res->resnorm = h.resnorm;
+    res->axnorm = h.axnorm;
+    res->niter = h.iter + niter_lo;
+    res->niter_lo = niter_lo;
+    (void)matvec_lo;
+    res->matvecs = 0;
+    res->converged = h.converged;
+    res->status = h.status ? h.status : (h.converged ? RQ_OK : RQ_E_MAXITER);
+    return RQ_OK;
+}
+
+__global__ void k_eig3_abi(const double *m, double *out) {
+    // m row-major complex [3][3]
+    auto at = [&](int r, int c) { return make_double2(m[2 * (3 * r + c)], m[2 * (3 * r + c) + 1]); };
+    double lam;
+    double2 v[3];
+    eig3(at(1, 0), at(2, 0), at(2, 1), at(0, 0), at(1, 1), at(2, 2), lam, v);
+    out[0] = lam;
+    out[1] = 0.;
+    for (int k = 0; k < 3; ++k) {
+        out[2 + 2 * k] = v[k].x;
+        out[3 + 2 * k] = v[k].y;
+    }
+}
+
+}  // namespace
+
+}  // namespace rq
+
+using namespace rq;
+
+RQ_API int rq_lobpcg_workspace_size(int64_t D, const rq_lobpcg_params_t *prm, size_t *bytes) {
+    if (!prm || !bytes || D < 1) return fail(RQ_E_ARG, "rq_lobpcg_workspace_size: bad arguments");
+    if (vtype_size(prm->vtype) == 0) return fail(RQ_E_ARG, "rq_lobpcg_workspace_size: bad vtype");
+    *bytes = layout(D, *prm).total;
+    return RQ_OK;
+}
+
+namespace rq {
+namespace {
+int solve_entry(const rq_operator_t *op, rq_matvec_fn fn, void *ctx, const rq_lobpcg_params_t *prm,
+                void *workspace, const void *x0, void *x_out, rq_lobpcg_result_t *res,
+                void *stream) {
+    if (!op || !prm || !workspace || !x0 || !x_out || !res)
+        return fail(RQ_E_ARG, "rq_lobpcg_solve: null argument");
+    if (prm->maxiter < 0) return fail(RQ_E_ARG, "rq_lobpcg_solve: maxiter < 0");
+    if (prm->variant != RQ_LOBPCG_REFERENCE && prm->variant != RQ_LOBPCG_FAST)
+        return fail(RQ_E_ARG, "rq_lobpcg_solve: unknown variant");
+    const int32_t vt = prm->vtype;
+    if (!fn && (vt == RQ_F32 || vt == RQ_F64) && !op->terms.is_real)
+        return fail(RQ_E_ARG, "rq_lobpcg_solve: real vectors need real coefficients");
+    if (op->sub.D < 1) return fail(RQ_E_ARG, "rq_lobpcg_solve: D must be >= 1");
+    std::memset(res, 0, sizeof(*res));
+    cudaStream_t user = as_stream(stream);
+    // graphs cannot be captured on the legacy default stream: use a private stream ordered
+    // after the caller's work
+    cudaStream_t s = user;
+    cudaStream_t priv = nullptr;
+    const bool graph = prm->use_graph && !fn;
+    if (graph && user == nullptr) {
+        RQ_CUDA(cudaStreamCreateWithFlags(&priv, cudaStreamNonBlocking));
+        RQ_CUDA(cudaDeviceSynchronize());
+        s = priv;
+    }
+    char *ws = static_cast<char *>(workspace);
+    int rc;
+    switch (vt) {
+        case RQ_F32: rc = solve<float, float>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
+        case RQ_F64: rc = solve<float, double>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
+        case RQ_C64: rc = solve<float2, float2>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
+        case RQ_C128: rc = solve<float2, double2>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
+        default: rc = fail(RQ_E_ARG, "rq_lobpcg_solve: bad vtype");
+    }
+    if (priv) {
+        cudaStreamSynchronize(priv);
+        cudaStreamDestroy(priv);
+    }
+    return rc;
+}
+}  // namespace
+}  // namespace rq
+
+RQ_API int rq_lobpcg_solve(const rq_operator_t *op, const rq_lobpcg_params_t *prm, void *workspace,
+                           const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream) {
+    return solve_entry(op, nullptr, nullptr, prm, workspace, x0, x_out, res, stream);
+}
+
+RQ_API int rq_lobpcg_solve_cb(int64_t D, rq_matvec_fn fn, void *ctx, const rq_lobpcg_params_t *prm,
+                              void *workspace, const void *x0, void *x_out, rq_lobpcg_result_t *res,
+                              void *stream) {
+    if (!fn) return fail(RQ_E_ARG, "rq_lobpcg_solve_cb: null callback");
+    if (prm && prm->variant != RQ_LOBPCG_REFERENCE)
+        return fail(RQ_E_ARG, "rq_lobpcg_solve_cb: callbacks run the REFERENCE variant");
+    rq_operator_t op = {};
+    op.sub.D = D;
+    op.terms.diag_group = -1;
+    op.terms.is_real = 1;
+    return solve_entry(&op, fn, ctx, prm, workspace, x0, x_out, res, stream);
+}
+
+RQ_API int rq_eigenpair_3x3(const double *mat, double *out, void *stream) {
+    if (!mat || !out) return fail(RQ_E_ARG, "rq_eigenpair_3x3: null argument");
+    k_eig3_abi<<<1, 1, 0, as_stream(stream)>>>(mat, out);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}

@@ -1,0 +1,624 @@
+// Pauli-sum matvec restricted to a sorted subspace (rqutils/sqd.py:578-684) and the full-space
+// form (rqutils/paulis/symplectic.py:131-150).
+//
+// Row-side formula: (H x)[i] = sum_j d_j(S[i]) x[m_j(i)],  d_j(s) = sum_k c_jk (-1)^popcount(s & z_jk),
+// S[m_j(i)] = S[i] ^ x_j (term dropped when absent).  One thread owns one row; the X masks,
+// offsets, Z masks and coefficients of a tile of groups sit in shared memory and every thread of
+// the block walks the same group sequence (broadcast reads).  Lookups of four groups are issued
+// together (four independent 32-byte bucket loads in flight per thread).  d_j is only evaluated
+// on a hit; the x = 0 group's diagonal is either read from a cached FP64 array or computed.
+//
+// Modes: FREE (lookups every call, cache_level (0, *)), CONN (cached (row -> source, group)
+// lists, diagonals recomputed, cache_level (1, 0)), CSR (cached element values, (*, 2)).
+#include <cmath>
+
+#include "rq_common.cuh"
+#include "rq_host.h"
+
+namespace rq {
+
+namespace {
+
+constexpr int kGT = 512;      // max groups per shared-memory tile
+constexpr int kKT = 2048;     // max terms per shared-memory tile
+constexpr int kSample = 2048; // shared-memory sample of the binary-search lookup
+constexpr int kFilterBytes = 544;
+
+template <typename R>
+struct Tile {
+    uint64_t *xm;
+    int32_t *off;
+    uint64_t *zm;
+    cx<R> *cf;
+};
+
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+template <typename R>
+__host__ __device__ inline size_t tile_bytes(int gt, int kt) {
+    return align16((size_t)gt * 8) + align16((size_t)(gt + 1) * 4) + align16((size_t)kt * 8) +
+           (size_t)kt * sizeof(cx<R>);
+}
+
+template <typename R>
+__device__ inline Tile<R> carve(unsigned char *p, int gt, int kt) {
+    Tile<R> t;
+    t.xm = reinterpret_cast<uint64_t *>(p);
+    p += align16((size_t)gt * 8);
+    t.off = reinterpret_cast<int32_t *>(p);
+    p += align16((size_t)(gt + 1) * 4);
+    t.zm = reinterpret_cast<uint64_t *>(p);
+    p += align16((size_t)kt * 8);
+    t.cf = reinterpret_cast<cx<R> *>(p);
+    return t;
+}
+
+// Stage groups [g0, g1) into shared memory, g1 as large as the tile allows.  Returns g1, or -1
+// when group g0 alone exceeds the tile.  Every thread of the block must call it.
+template <typename R>
+__device__ int load_tile(const rq_terms_t &T, int g0, int gt, int kt, const Tile<R> &tl,
+                         int *s_g1) {
+    __syncthreads();  // previous tile no longer in use
+    if (threadIdx.x == 0) *s_g1 = g0;
+    __syncthreads();
+    const int base = T.toff[g0];
+    const int gmax = min(T.J, g0 + gt);
+    for (int g = g0 + 1 + threadIdx.x; g <= gmax; g += blockDim.x)
+        if (T.toff[g] - base <= kt) atomicMax(s_g1, g);
+    __syncthreads();
+    const int g1 = *s_g1;
+    if (g1 == g0) return -1;
+    const int ng = g1 - g0;
+    const int nk = T.toff[g1] - base;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) tl.xm[g] = T.xmask[g0 + g];
+    for (int g = threadIdx.x; g <= ng; g += blockDim.x) tl.off[g] = T.toff[g0 + g] - base;
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+        tl.zm[k] = T.zmask[base + k];
+        tl.cf[k] = {(R)T.coef[2 * (base + k)], (R)T.coef[2 * (base + k) + 1]};
+    }
+    __syncthreads();
+    return g1;
+}
+
+// d_j(s) * xv accumulated into acc; the group's terms end at the first zero coefficient when
+// stop_at_zero (subspace form) and run to the end otherwise (full-space form).
+template <typename R>
+__device__ __forceinline__ void add_group(const cx<R> *cf, const uint64_t *zm, int k0, int k1,
+                                          uint64_t s, cx<R> xv, bool stop_at_zero, CAcc<R> &acc) {
+    CAcc<R> d;
+    for (int k = k0; k < k1; ++k) {
+        const cx<R> c = cf[k];
+        if (stop_at_zero && c.re == (R)0 && c.im == (R)0) break;
+        if (__popcll(s & zm[k]) & 1) d.add({-c.re, -c.im});
+        else d.add(c);
+    }
+    acc.add(cmul(d.get(), xv));
+}
+
+// Visit the hits of row state s over groups [g0, g1) (xm indexed by g - g0), skipping `skip`.
+// on_hit(g, m) is called in ascending g.
+template <int LK, typename F>
+__device__ __forceinline__ void for_hits(const rq_subspace_t &S, const uint32_t *fb,
+                                         const uint64_t *samp, int ns, const uint64_t *xm, int g0,
+                                         int g1, int skip, uint64_t s, int *err, F &&on_hit) {
+    int g = g0;
+    if (LK == RQ_LOOKUP_HASH) {
+        for (; g + 4 <= g1; g += 4) {
+            uint64_t t[4], b[4], k0[4], k1[4], k2[4], k3[4];
+            bool q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                t[u] = s ^ xm[g + u - g0];
+                q[u] = (g + u != skip) && (t[u] != S.empty_key) &&
+                       sector_ok(fb, S.fmask_a, S.fmask_b, t[u]);
+                b[u] = bucket_of(t[u], S.hbits);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (q[u]) load_bucket(S.hkeys + (b[u] << 2), k0[u], k1[u], k2[u], k3[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!q[u]) continue;
+                bool open;
+                const int sl = match_bucket(t[u], S.empty_key, k0[u], k1[u], k2[u], k3[u], open);
+                int m;
+                if (sl >= 0) m = __ldg(S.hvals + (b[u] << 2) + sl);
+                else if (open) m = -1;
+                else m = probe_rest(S, t[u], b[u], err);
+                if (m >= 0) on_hit(g + u, (int64_t)m);
+            }
+        }
+    }
+    for (; g < g1; ++g) {
+        if (g == skip) continue;
+        const uint64_t t = s ^ xm[g - g0];
+        int64_t m;
+        if (LK == RQ_LOOKUP_IDENTITY) {
+            m = (t < (uint64_t)S.D) ? (int64_t)t : -1;
+        } else {
+            if (!sector_ok(fb, S.fmask_a, S.fmask_b, t)) continue;
+            m = (LK == RQ_LOOKUP_HASH) ? lookup_hash(S, t, err) : lookup_bsearch(S, samp, ns, t);
+        }
+        if (m >= 0) on_hit(g, m);
+    }
+}
+
+template <int LK>
+__device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, uint64_t *samp,
+                                        int ns) {
+    if (LK != RQ_LOOKUP_IDENTITY)
+        for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) fb[w] = S.fbits[w];
+    if (LK == RQ_LOOKUP_BSEARCH)
+        for (int k = threadIdx.x; k < ns; k += blockDim.x)
+            samp[k] = S.states[((int64_t)k * S.D) / ns];
+}
+
+// ------------------------------------------------------------------------------------------
+// FREE mode
+// ------------------------------------------------------------------------------------------
+template <typename V, int LK>
+__global__ void __launch_bounds__(kThreads)
+k_matvec_free(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int gt, int kt,
+              int stop_at_zero, int *err, const int *gate, const int *gate2) {
+    using R = typename VT<V>::R;
+    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_g1;
+    const rq_subspace_t &S = op.sub;
+    const rq_terms_t &T = op.terms;
+    uint32_t *fb = reinterpret_cast<uint32_t *>(smem);
+    uint64_t *samp = reinterpret_cast<uint64_t *>(smem + kFilterBytes);
+    const int ns = (LK == RQ_LOOKUP_BSEARCH) ? (int)(S.D < kSample ? S.D : kSample) : 0;
+    const Tile<R> tl =
+        carve<R>(smem + kFilterBytes + (LK == RQ_LOOKUP_BSEARCH ? kSample * 8 : 0), gt, kt);
+    load_lookup_smem<LK>(S, fb, samp, ns);
+
+    const int64_t D = S.D;
+    const bool d0 = (op.diag0 != nullptr) && (T.diag_group >= 0);
+    const int gstart = (d0 && T.diag_group == 0) ? 1 : 0;
+    const int skip = T.diag_group;  // handled outside the hit loop
+    int g1_first = (gstart < T.J) ? load_tile<R>(T, gstart, gt, kt, tl, &s_g1) : T.J;
+    if (g1_first < 0) {
+        if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
+        return;
+    }
+    const bool resident = (g1_first >= T.J);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < D;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const bool active = i < D;
+        const uint64_t s =
+            active ? (LK == RQ_LOOKUP_IDENTITY ? (uint64_t)i : __ldg(S.states + i)) : 0ULL;
+        CAcc<R> acc;
+        if (active && d0) {
+            const R dv = (R)op.diag0[i];
+            const cx<R> xv = VT<V>::ld(x, i);
+            acc.add({dv * xv.re, dv * xv.im});
+        }
+        if (!resident && base != (int64_t)blockIdx.x * blockDim.x)
+            g1_first = load_tile<R>(T, gstart, gt, kt, tl, &s_g1);
+        int g0 = gstart, g1 = g1_first;
+        while (g0 < T.J) {
+            if (g1 < 0) {
+                if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
+                return;  // uniform across the block
+            }
+            if (active) {
+                if (!d0 && skip >= g0 && skip < g1)
+                    add_group<R>(tl.cf, tl.zm, tl.off[skip - g0], tl.off[skip - g0 + 1], s,
+                                 VT<V>::ld(x, i), stop_at_zero, acc);
+                for_hits<LK>(S, fb, samp, ns, tl.xm, g0, g1, skip, s, err,
+                             [&](int g, int64_t m) {
+                                 add_group<R>(tl.cf, tl.zm, tl.off[g - g0], tl.off[g - g0 + 1],
+                                              s, VT<V>::ld(x, m), stop_at_zero, acc);
+                             });
+            }
+            if (g1 >= T.J) break;
+            g0 = g1;
+            g1 = load_tile<R>(T, g0, gt, kt, tl, &s_g1);
+        }
+        if (active) VT<V>::st(y, i, acc.get());
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// connectivity cache
+// ------------------------------------------------------------------------------------------
+template <int LK>
+__global__ void __launch_bounds__(kThreads)
+k_conn_count(const rq_operator_t op, int64_t *__restrict__ rowcnt, int *err) {
+    __shared__ uint32_t fb[RQ_FILTER_WORDS];
+    __shared__ uint64_t samp[LK == RQ_LOOKUP_BSEARCH ? kSample : 1];
+    const rq_subspace_t &S = op.sub;
+    const int ns = (LK == RQ_LOOKUP_BSEARCH) ? (int)(S.D < kSample ? S.D : kSample) : 0;
+    load_lookup_smem<LK>(S, fb, samp, ns);
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = 0;
+        for_hits<LK>(S, fb, samp, ns, op.terms.xmask, 0, op.terms.J, op.terms.diag_group,
+                     __ldg(S.states + i), err, [&](int, int64_t) { ++c; });
+        rowcnt[i] = c;
+    }
+}
+
+// Diagonal of group g for state s from the global term arrays (CONN mode and CSR values).
+template <typename R>
+__device__ __forceinline__ cx<R> group_diag(const rq_terms_t &T, int g, uint64_t s) {
+    CAcc<R> d;
+    const int k1 = __ldg(T.toff + g + 1);
+    for (int k = __ldg(T.toff + g); k < k1; ++k) {
+        const R re = (R)__ldg(T.coef + 2 * k), im = (R)__ldg(T.coef + 2 * k + 1);
+        if (re == (R)0 && im == (R)0) break;
+        if (__popcll(s & __ldg(T.zmask + k)) & 1) d.add({-re, -im});
+        else d.add({re, im});
+    }
+    return d.get();
+}
+
+template <typename V, int LK>
+__global__ void __launch_bounds__(kThreads)
+k_conn_fill(const rq_operator_t op, const int64_t *__restrict__ rowptr, int32_t *__restrict__ col,
+            int32_t *__restrict__ grp, V *__restrict__ val, int *err) {
+    using R = typename VT<V>::R;
+    __shared__ uint32_t fb[RQ_FILTER_WORDS];
+    __shared__ uint64_t samp[LK == RQ_LOOKUP_BSEARCH ? kSample : 1];
+    const rq_subspace_t &S = op.sub;
+    const int ns = (LK == RQ_LOOKUP_BSEARCH) ? (int)(S.D < kSample ? S.D : kSample) : 0;
+    load_lookup_smem<LK>(S, fb, samp, ns);
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = rowptr[i];
+        const uint64_t s = __ldg(S.states + i);
+        for_hits<LK>(S, fb, samp, ns, op.terms.xmask, 0, op.terms.J, op.terms.diag_group, s, err,
+                     [&](int g, int64_t m) {
+                         col[p] = (int32_t)m;
+                         if (grp) grp[p] = g;
+                         if (val) VT<V>::st(val, p, group_diag<R>(op.terms, g, s));
+                         ++p;
+                     });
+    }
+}
+
+// Inclusive scan of rowptr[1..D] in place (three phases: block scans, scan of block totals,
+// add block offsets).  Block b covers rows [b * 1024, (b + 1) * 1024).
+__global__ void __launch_bounds__(kThreads) k_scan_blocks(int64_t *v, int64_t n, int64_t *bsum) {
+    __shared__ int64_t ws[kThreads / 32];
+    const int64_t base = (int64_t)blockIdx.x * 1024;
+    int64_t loc[4];
+    int64_t t = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int64_t idx = base + threadIdx.x * 4 + k;
+        loc[k] = (idx < n) ? v[idx] : 0;
+        t += loc[k];
+    }
+    // exclusive scan of per-thread totals across the block
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t inc = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) ws[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        int64_t w = (lane < kThreads / 32) ? ws[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        if (lane < kThreads / 32) ws[lane] = w;
+    }
+    __syncthreads();
+    int64_t run = inc - t + (warp > 0 ? ws[warp - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int64_t idx = base + threadIdx.x * 4 + k;
+        run += loc[k];
+        if (idx < n) v[idx] = run;
+    }
+    if (threadIdx.x == kThreads - 1) bsum[blockIdx.x] = run;
+}
+
+__global__ void k_scan_totals(int64_t *bsum, int64_t nb) {
+    // one block: sequential chunks per thread, then a block scan of chunk totals
+    __shared__ int64_t tot[kThreads];
+    const int64_t per = (nb + blockDim.x - 1) / blockDim.x;
+    const int64_t a = threadIdx.x * per, b = min(nb, a + per);
+    int64_t s = 0;
+    for (int64_t k = a; k < b; ++k) s += bsum[k];
+    tot[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t r = 0;
+        for (int k = 0; k < (int)blockDim.x; ++k) {
+            const int64_t u = tot[k];
+            tot[k] = r;
+            r += u;
+        }
+    }
+    __syncthreads();
+    int64_t r = tot[threadIdx.x];
+    for (int64_t k = a; k < b; ++k) {  // exclusive offsets of blocks
+        const int64_t u = bsum[k];
+        bsum[k] = r;
+        r += u;
+    }
+}
+
+__global__ void k_scan_add(int64_t *v, int64_t n, const int64_t *boff) {
+    const int64_t base = (int64_t)blockIdx.x * 1024;
+    const int64_t off = boff[blockIdx.x];
+    for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
+        const int64_t idx = base + k;
+        if (idx < n) v[idx] += off;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// CONN and CSR modes
+// ------------------------------------------------------------------------------------------
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+k_matvec_conn(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, const int *gate,
+              const int *gate2) {
+    using R = typename VT<V>::R;
+    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
+    const rq_terms_t &T = op.terms;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.sub.D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = __ldg(op.sub.states + i);
+        CAcc<R> acc;
+        const cx<R> xi = VT<V>::ld(x, i);
+        if (op.diag0) {
+            const R dv = (R)op.diag0[i];
+            acc.add({dv * xi.re, dv * xi.im});
+        } else if (T.diag_group >= 0) {
+            acc.add(cmul(group_diag<R>(T, T.diag_group, s), xi));
+        }
+        const int64_t e1 = op.rowptr[i + 1];
+        for (int64_t e = op.rowptr[i]; e < e1; ++e)
+            acc.add(cmul(group_diag<R>(T, __ldg(op.grp + e), s), VT<V>::ld(x, __ldg(op.col + e))));
+        VT<V>::st(y, i, acc.get());
+    }
+}
+
+// VV: storage type of the element values (converted to the vector's precision on load)
+template <typename V, typename VV>
+__global__ void __launch_bounds__(kThreads)
+k_matvec_csr(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, const int *gate,
+             const int *gate2) {
+    using R = typename VT<V>::R;
+    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
+    const VV *val = reinterpret_cast<const VV *>(op.val);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.sub.D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        CAcc<R> acc;
+        if (op.diag0) {
+            const R dv = (R)op.diag0[i];
+            const cx<R> xi = VT<V>::ld(x, i);
+            acc.add({dv * xi.re, dv * xi.im});
+        }
+        const int64_t e1 = op.rowptr[i + 1];
+        for (int64_t e = op.rowptr[i]; e < e1; ++e) {
+            const auto v = VT<VV>::ld(val, e);
+            acc.add(cmul(cx<R>{(R)v.re, (R)v.im}, VT<V>::ld(x, __ldg(op.col + e))));
+        }
+        VT<V>::st(y, i, acc.get());
+    }
+}
+
+template <typename V>
+int launch_csr(const rq_operator_t &op, const void *x, void *y, cudaStream_t st, const int *gate,
+               const int *gate2, int grid) {
+    const V *xx = static_cast<const V *>(x);
+    V *yy = static_cast<V *>(y);
+    switch (op.val_vtype) {
+        case RQ_F32: k_matvec_csr<V, float><<<grid, kThreads, 0, st>>>(op, xx, yy, gate, gate2); break;
+        case RQ_F64: k_matvec_csr<V, double><<<grid, kThreads, 0, st>>>(op, xx, yy, gate, gate2); break;
+        case RQ_C64:
+            if (!VT<V>::kComplex) return fail(RQ_E_ARG, "rq_matvec: complex CSR values need complex vectors");
+            k_matvec_csr<V, float2><<<grid, kThreads, 0, st>>>(op, xx, yy, gate, gate2);
+            break;
+        case RQ_C128:
+            if (!VT<V>::kComplex) return fail(RQ_E_ARG, "rq_matvec: complex CSR values need complex vectors");
+            k_matvec_csr<V, double2><<<grid, kThreads, 0, st>>>(op, xx, yy, gate, gate2);
+            break;
+        default: return fail(RQ_E_ARG, "rq_matvec: bad val_vtype");
+    }
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// host dispatch
+// ------------------------------------------------------------------------------------------
+template <typename V, int LK>
+int launch_free(const rq_operator_t &op, const void *x, void *y, int stop_at_zero, int *err,
+                cudaStream_t st, const int *gate = nullptr, const int *gate2 = nullptr) {
+    using R = typename VT<V>::R;
+    const rq_terms_t &T = op.terms;
+    const int gt = T.J < kGT ? (T.J > 0 ? T.J : 1) : kGT;
+    const int kt = T.K < kKT ? (T.K > 0 ? T.K : 1) : kKT;
+    const size_t smem = kFilterBytes + (LK == RQ_LOOKUP_BSEARCH ? kSample * 8 : 0) +
+                        tile_bytes<R>(gt, kt);
+    auto kern = k_matvec_free<V, LK>;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    // occupancy query cached per instantiation and shared-memory size (it is also reached while a
+    // stream is being captured, where only stream work should be issued)
+    static size_t occ_smem = ~size_t(0);
+    static int occ_blocks = 1;
+    if (occ_smem != smem) {
+        int per = 0;
+        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, smem));
+        occ_blocks = per < 1 ? 1 : per;
+        occ_smem = smem;
+    }
+    const int per_sm = occ_blocks;
+    int64_t g = (op.sub.D + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
+    if (g > cap) g = cap;
+    kern<<<(int)g, kThreads, smem, st>>>(op, static_cast<const V *>(x), static_cast<V *>(y), gt, kt,
+                                         stop_at_zero, err, gate, gate2);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}
+
+int grid_rows(int64_t n) {
+    int64_t g = (n + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    return (int)(g > cap ? cap : (g < 1 ? 1 : g));
+}
+
+template <typename V>
+int matvec_typed(const rq_operator_t &op, const void *x, void *y, void *scratch, cudaStream_t st,
+                 const int *gate, const int *gate2) {
+    int *err = scratch ? scratch_err(scratch) : nullptr;
+    switch (op.mode) {
+        case RQ_MODE_FREE:
+            if (op.sub.lookup == RQ_LOOKUP_HASH)
+                return launch_free<V, RQ_LOOKUP_HASH>(op, x, y, 1, err, st, gate, gate2);
+            if (op.sub.lookup == RQ_LOOKUP_BSEARCH)
+                return launch_free<V, RQ_LOOKUP_BSEARCH>(op, x, y, 1, err, st, gate, gate2);
+            return fail(RQ_E_ARG, "rq_matvec: unsupported lookup for a subspace");
+        case RQ_MODE_CONN:
+            if (!op.rowptr || (op.nnz > 0 && (!op.col || !op.grp)))
+                return fail(RQ_E_ARG, "rq_matvec: RQ_MODE_CONN needs rowptr, col and grp");
+            k_matvec_conn<V><<<grid_rows(op.sub.D), kThreads, 0, st>>>(
+                op, static_cast<const V *>(x), static_cast<V *>(y), gate, gate2);
+            RQ_CUDA(cudaGetLastError());
+            return RQ_OK;
+        case RQ_MODE_CSR:
+            if (!op.rowptr || (op.nnz > 0 && (!op.col || !op.val)))
+                return fail(RQ_E_ARG, "rq_matvec: RQ_MODE_CSR needs rowptr, col and val");
+            if (op.terms.diag_group >= 0 && !op.diag0)
+                return fail(RQ_E_ARG, "rq_matvec: RQ_MODE_CSR needs diag0 when a diagonal group exists");
+            return launch_csr<V>(op, x, y, st, gate, gate2, grid_rows(op.sub.D));
+        default:
+            return fail(RQ_E_ARG, "rq_matvec: unknown mode");
+    }
+}
+
+int check_operator(const rq_operator_t *op, int32_t vtype) {
+    if (!op) return fail(RQ_E_ARG, "null operator");
+    const rq_terms_t &T = op->terms;
+    if (T.J < 0 || T.K < 0 || (T.J > 0 && (!T.xmask || !T.toff)) || (T.K > 0 && (!T.zmask || !T.coef)))
+        return fail(RQ_E_ARG, "terms: bad sizes or null arrays");
+    if (T.diag_group >= T.J) return fail(RQ_E_ARG, "terms: diag_group out of range");
+    if ((vtype == RQ_F32 || vtype == RQ_F64) && !T.is_real)
+        return fail(RQ_E_ARG, "real vectors need real coefficients (terms.is_real)");
+    if (vtype_size(vtype) == 0) return fail(RQ_E_ARG, "unknown value type");
+    if (op->sub.D < 1 || op->sub.D >= (int64_t(1) << 31))
+        return fail(RQ_E_RANGE, "subspace dimension must be in [1, 2^31)");
+    return RQ_OK;
+}
+
+}  // namespace
+
+// entry used by the LOBPCG driver (same translation-unit-independent dispatch)
+int matvec_dispatch(const rq_operator_t &op, int32_t vtype, const void *x, void *y, void *scratch,
+                    cudaStream_t st, const int *gate, const int *gate2) {
+    switch (vtype) {
+        case RQ_F32: return matvec_typed<float>(op, x, y, scratch, st, gate, gate2);
+        case RQ_F64: return matvec_typed<double>(op, x, y, scratch, st, gate, gate2);
+        case RQ_C64: return matvec_typed<float2>(op, x, y, scratch, st, gate, gate2);
+        case RQ_C128: return matvec_typed<double2>(op, x, y, scratch, st, gate, gate2);
+        default: return fail(RQ_E_ARG, "unknown value type");
+    }
+}
+
+}  // namespace rq
+
+using namespace rq;
+
+RQ_API int rq_matvec(const rq_operator_t *op, int32_t vtype, const void *x, void *y, void *scratch,
+                     void *stream) {
+    RQ_TRY(check_operator(op, vtype));
+    if (!x || !y || x == y) return fail(RQ_E_ARG, "rq_matvec: x and y must be distinct non-null");
+    if (op->mode == RQ_MODE_FREE && !scratch)
+        return fail(RQ_E_ARG, "rq_matvec: RQ_MODE_FREE needs scratch (error flag)");
+    return matvec_dispatch(*op, vtype, x, y, scratch, as_stream(stream), nullptr, nullptr);
+}
+
+RQ_API int rq_fullspace_matvec(const rq_terms_t *terms, int32_t n, int32_t vtype, const void *x,
+                               void *y, void *stream) {
+    if (!terms || !x || !y || x == y || n < 0 || n > 31)
+        return fail(RQ_E_ARG, "rq_fullspace_matvec: bad arguments (n must be <= 31)");
+    rq_operator_t op = {};
+    op.terms = *terms;
+    op.terms.diag_group = -1;  // the x = 0 group is handled like any other (source = row)
+    op.sub.D = int64_t(1) << n;
+    op.sub.lookup = RQ_LOOKUP_IDENTITY;
+    op.mode = RQ_MODE_FREE;
+    RQ_TRY(check_operator(&op, vtype));
+    cudaStream_t st = as_stream(stream);
+    // PauliSumXZ.matmul sums every stored coefficient (no stop at a zero), symplectic.py:142-147
+    switch (vtype) {
+        case RQ_F32: return launch_free<float, RQ_LOOKUP_IDENTITY>(op, x, y, 0, nullptr, st);
+        case RQ_F64: return launch_free<double, RQ_LOOKUP_IDENTITY>(op, x, y, 0, nullptr, st);
+        case RQ_C64: return launch_free<float2, RQ_LOOKUP_IDENTITY>(op, x, y, 0, nullptr, st);
+        case RQ_C128: return launch_free<double2, RQ_LOOKUP_IDENTITY>(op, x, y, 0, nullptr, st);
+        default: return fail(RQ_E_ARG, "unknown value type");
+    }
+}
+
+RQ_API int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col, int32_t *grp,
+                         void *val, int32_t vtype, int64_t *nnz, void *scratch, void *stream) {
+    RQ_TRY(check_operator(op, val ? vtype : RQ_C128));
+    if (!rowptr || !scratch || !nnz) return fail(RQ_E_ARG, "rq_conn_build: null argument");
+    const rq_subspace_t &S = op->sub;
+    if (S.lookup != RQ_LOOKUP_HASH && S.lookup != RQ_LOOKUP_BSEARCH)
+        return fail(RQ_E_ARG, "rq_conn_build: needs a hash or binary-search subspace");
+    cudaStream_t st = as_stream(stream);
+    int *err = scratch_err(scratch);
+    const int64_t D = S.D;
+    if (!col) {
+        RQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        RQ_CUDA(cudaMemsetAsync(rowptr, 0, sizeof(int64_t), st));
+        if (S.lookup == RQ_LOOKUP_HASH)
+            k_conn_count<RQ_LOOKUP_HASH><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
+        else
+            k_conn_count<RQ_LOOKUP_BSEARCH><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
+        RQ_CUDA(cudaGetLastError());
+        const int64_t nb = (D + 1023) / 1024;
+        int64_t *bsum = scratch_scan(scratch);
+        k_scan_blocks<<<(int)nb, kThreads, 0, st>>>(rowptr + 1, D, bsum);
+        k_scan_totals<<<1, kThreads, 0, st>>>(bsum, nb);
+        k_scan_add<<<(int)nb, kThreads, 0, st>>>(rowptr + 1, D, bsum);
+        RQ_CUDA(cudaGetLastError());
+        int h_err = 0;
+        RQ_CUDA(cudaMemcpyAsync(nnz, rowptr + D, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaStreamSynchronize(st));
+        if (h_err) return fail(h_err, "rq_conn_build: lookup failed");
+        return RQ_OK;
+    }
+    const int g = grid_rows(D);
+#define RQ_FILL(V)                                                                                  \
+    do {                                                                                            \
+        if (S.lookup == RQ_LOOKUP_HASH)                                                             \
+            k_conn_fill<V, RQ_LOOKUP_HASH><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,           \
+                                                                   static_cast<V *>(val), err);     \
+        else                                                                                        \
+            k_conn_fill<V, RQ_LOOKUP_BSEARCH><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,        \
+                                                                      static_cast<V *>(val), err);  \
+    } while (0)
+    switch (val ? vtype : RQ_C128) {
+        case RQ_F32: RQ_FILL(float); break;
+        case RQ_F64: RQ_FILL(double); break;
+        case RQ_C64: RQ_FILL(float2); break;
+        case RQ_C128: RQ_FILL(double2); break;
+        default: return fail(RQ_E_ARG, "rq_conn_build: unknown value type");
+    }
+#undef RQ_FILL
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}

@@ -1,0 +1,247 @@
+// Subspace construction and per-group lookups:
+//   rq_subspace_build  -- strict-increase check, empty-key choice, hash table, sector filter
+//   rq_xsource         -- get_xsource (rqutils/sqd.py:448-503) for any number of X masks
+//   rq_diagonal        -- get_diagonal (rqutils/sqd.py:554-575), stopping at the first zero
+#include "rq_common.cuh"
+#include "rq_host.h"
+
+namespace rq {
+
+namespace {
+
+__global__ void k_check_sorted(const uint64_t *__restrict__ s, int64_t D, int *flag,
+                               unsigned long long *gap) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i + 1 < D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = s[i], b = s[i + 1];
+        if (a >= b) atomicExch(flag, 1);
+        if (b != a + 1) atomicMin(gap, (unsigned long long)i);
+    }
+}
+
+__global__ void k_fill_u64(uint64_t *p, int64_t n, uint64_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// Insert every state into its bucket chain: claim the first empty slot with a CAS.  Keys are
+// distinct, so a failed CAS always means "occupied by another key".  Slots of a bucket are
+// claimed in order, which keeps the occupied slots a prefix of the bucket.
+__global__ void k_hash_insert(const uint64_t *__restrict__ states, int64_t D,
+                              unsigned long long *keys, int32_t *vals, int hbits,
+                              unsigned long long empty, int *err) {
+    const uint64_t mask = (1ULL << hbits) - 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = states[i];
+        uint64_t b = bucket_of(key, hbits);
+        bool done = false;
+        for (uint64_t n = 0; n <= mask && !done; ++n) {
+            unsigned long long *slot = keys + (b << 2);
+            for (int s = 0; s < 4; ++s) {
+                if (atomicCAS(slot + s, empty, key) == empty) {
+                    vals[(b << 2) + s] = (int32_t)i;
+                    done = true;
+                    break;
+                }
+            }
+            b = (b + 1) & mask;
+        }
+        if (!done) atomicExch(err, RQ_E_TABLE);
+    }
+}
+
+__global__ void k_filter_build(const uint64_t *__restrict__ s, int64_t D, uint64_t fa, uint64_t fb,
+                               uint32_t *bits) {
+    __shared__ uint32_t loc[RQ_FILTER_WORDS];
+    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) loc[w] = 0u;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = s[i];
+        const int bit = __popcll(v & fa) * 65 + __popcll(v & fb);
+        atomicOr(&loc[bit >> 5], 1u << (bit & 31));
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x)
+        if (loc[w]) atomicOr(bits + w, loc[w]);
+}
+
+constexpr int kSample = 2048;  // shared-memory sample size of the binary-search lookup
+
+template <int LK>
+__global__ void __launch_bounds__(kThreads)
+k_xsource(const rq_subspace_t S, const uint64_t *__restrict__ xm, int J, int32_t *__restrict__ out,
+          int *err) {
+    __shared__ uint32_t fb[RQ_FILTER_WORDS];
+    __shared__ uint64_t samp[LK == RQ_LOOKUP_BSEARCH ? kSample : 1];
+    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) fb[w] = S.fbits[w];
+    const int ns = (int)(S.D < kSample ? S.D : kSample);
+    if (LK == RQ_LOOKUP_BSEARCH)
+        for (int k = threadIdx.x; k < ns; k += blockDim.x) samp[k] = S.states[((int64_t)k * S.D) / ns];
+    __syncthreads();
+    const int64_t total = (int64_t)J * S.D;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / S.D);
+        const int64_t i = idx - (int64_t)j * S.D;
+        const uint64_t t = __ldg(S.states + i) ^ __ldg(xm + j);
+        int m = -1;
+        if (sector_ok(fb, S.fmask_a, S.fmask_b, t)) {
+            if (LK == RQ_LOOKUP_HASH) m = lookup_hash(S, t, err);
+            else m = lookup_bsearch(S, samp, ns, t);
+        }
+        out[idx] = m;
+    }
+}
+
+// get_diagonal with the reference's loop: terms in order, stop at the first zero coefficient.
+__global__ void __launch_bounds__(kThreads)
+k_diagonal(const uint64_t *__restrict__ s, int64_t D, const uint64_t *__restrict__ z,
+           const double *__restrict__ c, int K, double2 *__restrict__ out) {
+    constexpr int kChunk = 1024;
+    __shared__ uint64_t zs[kChunk];
+    __shared__ double cr[kChunk], ci[kChunk];
+    __shared__ int kstop;
+    if (threadIdx.x == 0) kstop = K;
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x)
+        if (c[2 * k] == 0. && c[2 * k + 1] == 0.) atomicMin(&kstop, k);
+    __syncthreads();
+    const int kend = kstop;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < D;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const uint64_t v = (i < D) ? s[i] : 0;
+        double re = 0., im = 0.;
+        for (int k0 = 0; k0 < kend; k0 += kChunk) {
+            const int n = min(kChunk, kend - k0);
+            __syncthreads();
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                zs[k] = z[k0 + k];
+                cr[k] = c[2 * (k0 + k)];
+                ci[k] = c[2 * (k0 + k) + 1];
+            }
+            __syncthreads();
+            for (int k = 0; k < n; ++k) {
+                const double sg = (__popcll(v & zs[k]) & 1) ? -1. : 1.;
+                re += sg * cr[k];
+                if (ci[k] != 0.) im += sg * ci[k];
+            }
+        }
+        if (i < D) out[i] = make_double2(re, im);
+    }
+}
+
+int grid_for(int64_t n, int per_sm = 8) {
+    int64_t g = (n + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+}  // namespace rq
+
+using namespace rq;
+
+RQ_API int rq_subspace_sizes(int64_t D, int32_t *hbits) {
+    if (!hbits || D < 1) return fail(RQ_E_ARG, "rq_subspace_sizes: D must be >= 1");
+    int b = 1;
+    while ((int64_t(1) << b) * 2 < D) ++b;  // buckets * 4 slots >= 2 D
+    *hbits = b;
+    return RQ_OK;
+}
+
+RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
+    if (!sub || !sub->states || !scratch) return fail(RQ_E_ARG, "rq_subspace_build: null argument");
+    const int64_t D = sub->D;
+    if (D < 1 || D >= (int64_t(1) << 31))
+        return fail(RQ_E_RANGE, "rq_subspace_build: D must be in [1, 2^31)");
+    if (sub->lookup != RQ_LOOKUP_HASH && sub->lookup != RQ_LOOKUP_BSEARCH)
+        return fail(RQ_E_ARG, "rq_subspace_build: lookup must be RQ_LOOKUP_HASH or RQ_LOOKUP_BSEARCH");
+    if (!sub->fbits) return fail(RQ_E_ARG, "rq_subspace_build: fbits is null");
+    if (sub->lookup == RQ_LOOKUP_HASH) {
+        if (!sub->hkeys || !sub->hvals || sub->hbits < 1 || sub->hbits > 40)
+            return fail(RQ_E_ARG, "rq_subspace_build: hash buffers missing or hbits out of range");
+        if ((int64_t(4) << sub->hbits) < D + 1)
+            return fail(RQ_E_ARG, "rq_subspace_build: hash table too small for D");
+    }
+    cudaStream_t st = as_stream(stream);
+    int *flag = scratch_err(scratch);
+    unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
+    RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    RQ_CUDA(cudaMemsetAsync(gap, 0xff, sizeof(unsigned long long), st));
+    k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, flag, gap);
+    RQ_CUDA(cudaGetLastError());
+    int h_flag = 0;
+    unsigned long long h_gap = 0;
+    uint64_t first = 0, last = 0;
+    RQ_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaMemcpyAsync(&h_gap, gap, sizeof(h_gap), cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaMemcpyAsync(&first, sub->states, 8, cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaMemcpyAsync(&last, sub->states + (D - 1), 8, cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaStreamSynchronize(st));
+    if (h_flag) return fail(RQ_E_UNSORTED, "rq_subspace_build: states are not strictly increasing");
+    uint64_t empty;
+    if (last != ~0ULL) {
+        empty = ~0ULL;
+    } else if (first != 0ULL) {
+        empty = 0ULL;
+    } else {  // both extremes present: the first gap exists because D < 2^64
+        uint64_t below = 0;
+        RQ_CUDA(cudaMemcpy(&below, sub->states + h_gap, 8, cudaMemcpyDeviceToHost));
+        empty = below + 1;
+    }
+    sub->empty_key = empty;
+    RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (sub->lookup == RQ_LOOKUP_HASH) {
+        const int64_t slots = int64_t(4) << sub->hbits;
+        k_fill_u64<<<grid_for(slots), kThreads, 0, st>>>(sub->hkeys, slots, empty);
+        k_hash_insert<<<grid_for(D), kThreads, 0, st>>>(
+            sub->states, D, reinterpret_cast<unsigned long long *>(sub->hkeys), sub->hvals,
+            sub->hbits, empty, flag);
+        RQ_CUDA(cudaGetLastError());
+    }
+    RQ_CUDA(cudaMemsetAsync(sub->fbits, 0, RQ_FILTER_WORDS * sizeof(uint32_t), st));
+    k_filter_build<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->fmask_a, sub->fmask_b,
+                                                      sub->fbits);
+    RQ_CUDA(cudaGetLastError());
+    RQ_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaStreamSynchronize(st));
+    if (h_flag) return fail(RQ_E_TABLE, "rq_subspace_build: hash insertion failed");
+    return RQ_OK;
+}
+
+RQ_API int rq_xsource(const rq_subspace_t *sub, const uint64_t *xmask, int32_t J, int32_t *out,
+                      void *stream) {
+    if (!sub || !xmask || !out || J < 0) return fail(RQ_E_ARG, "rq_xsource: bad arguments");
+    if (J == 0) return RQ_OK;
+    cudaStream_t st = as_stream(stream);
+    const int64_t total = (int64_t)J * sub->D;
+    const int g = grid_for(total);
+    // the error flag of a hash chain that never ends is dropped here (the table was validated
+    // at build time); a null pointer tells the lookup not to report
+    if (sub->lookup == RQ_LOOKUP_HASH)
+        k_xsource<RQ_LOOKUP_HASH><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
+    else if (sub->lookup == RQ_LOOKUP_BSEARCH)
+        k_xsource<RQ_LOOKUP_BSEARCH><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
+    else
+        return fail(RQ_E_ARG, "rq_xsource: unsupported lookup");
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}
+
+RQ_API int rq_diagonal(const uint64_t *states, int64_t D, const uint64_t *zmask, const double *coef,
+                       int32_t K, double *out, void *stream) {
+    if (!states || !out || D < 1 || K < 0 || (K > 0 && (!zmask || !coef)))
+        return fail(RQ_E_ARG, "rq_diagonal: bad arguments");
+    cudaStream_t st = as_stream(stream);
+    k_diagonal<<<grid_for(D, 4), kThreads, 0, st>>>(states, D, zmask, coef, K,
+                                                   reinterpret_cast<double2 *>(out));
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}

@@ -1,0 +1,69 @@
+"""The C ABI library builds, loads and exports exactly what include/rqsqd.h declares (CPU)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, 'include', 'rqsqd.h')
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    names = re.findall(r'^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(rq_[a-z0-9_]+)\s*\(', src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope='module')
+def libpath():
+    from rqutils_gb300._build import build
+    return build()
+
+
+def test_header_parses():
+    names = declared_functions()
+    assert 'rq_matvec' in names and 'rq_lobpcg_solve' in names and len(names) >= 14
+
+
+def test_exports_match_header(libpath):
+    out = subprocess.run(['nm', '-D', '--defined-only', libpath], capture_output=True, text=True,
+                         check=True).stdout
+    exported = sorted(set(re.findall(r' T (rq_[a-z0-9_]+)$', out, flags=re.M)))
+    assert exported == declared_functions()
+
+
+def test_ctypes_binding_covers_header(libpath):
+    from rqutils_gb300 import _lib as L
+    assert sorted(L.SIGNATURES) == declared_functions()
+    lib = L.lib()
+    assert lib.rq_version() >= 100
+    for name in declared_functions():
+        assert hasattr(lib, name)
+
+
+def test_host_only_entry_points(libpath):
+    """Sizing calls need no GPU."""
+    from rqutils_gb300 import _lib as L
+    lib = L.lib()
+    hb = ctypes.c_int32()
+    assert lib.rq_subspace_sizes(1 << 20, ctypes.byref(hb)) == 0
+    assert (4 << hb.value) >= 2 * (1 << 20)
+    n = ctypes.c_size_t()
+    assert lib.rq_scratch_size(1 << 20, ctypes.byref(n)) == 0 and n.value > 0
+    prm = L.LobpcgParams(maxiter=10, variant=0, vtype=L.C128, mixed=1)
+    assert lib.rq_lobpcg_workspace_size(1000, ctypes.byref(prm), ctypes.byref(n)) == 0
+    assert n.value >= 8 * 1000 * 24
+    assert lib.rq_subspace_sizes(0, ctypes.byref(hb)) == L.E_ARG
+    assert b'D must be' in lib.rq_last_error()
+
+
+def test_struct_layouts():
+    from rqutils_gb300 import _lib as L
+    assert ctypes.sizeof(L.Subspace) == 72
+    assert ctypes.sizeof(L.Terms) == 48
+    assert ctypes.sizeof(L.Operator) == 72 + 48 + 8 + 40 + 8
+    assert ctypes.sizeof(L.LobpcgParams) == 64
+    assert ctypes.sizeof(L.LobpcgResult) == 48

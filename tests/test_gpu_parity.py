@@ -1,0 +1,199 @@
+"""CUDA path against the reference fixtures and the oracle (GPU)."""
+import warnings
+
+import numpy as np
+import pytest
+
+from golden_cases import case_names, load, hamiltonian
+
+pytestmark = pytest.mark.gpu
+
+CASES = case_names()
+CONVERGING = [c for c in CASES if c not in ('local20', 'n16')]
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from rqutils_gb300._build import build
+    build()
+
+
+def _problem(case, cache_level=(1, 0), lookup='hash'):
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    from rqutils_gb300.sqd import SQDProblem, subspace_states
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        h = PauliSumXZ.from_paulisum(hamiltonian(case), force_real=True, add_padding=True)
+    S = subspace_states(case['states'], h.num_qubits)
+    return SQDProblem(h, S, cache_level=cache_level, lookup=lookup), h, S
+
+
+@pytest.mark.parametrize('lookup', ['hash', 'bsearch'])
+@pytest.mark.parametrize('name', CASES)
+def test_xsource_bit_exact(name, lookup):
+    case = load(name)
+    prob, h, S = _problem(case, cache_level=(0, 0), lookup=lookup)
+    D = int(case['D'])
+    got = prob.sub.xsource(h.xmask).cpu().numpy()
+    np.testing.assert_array_equal(got, case['xsources'][:, :D])
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_group_diagonals(name):
+    case = load(name)
+    prob, h, S = _problem(case, cache_level=(0, 0))
+    D = int(case['D'])
+    for j in range(len(h.xmask)):
+        d = prob.op.group_diagonal(j).cpu().numpy()
+        ref = case['diagonals'][j, :D]
+        np.testing.assert_allclose(d if np.iscomplexobj(ref) else d.real, ref, rtol=1e-13,
+                                   atol=1e-13)
+
+
+@pytest.mark.parametrize('mode', [(0, 0), (1, 0), (1, 2)])
+@pytest.mark.parametrize('name', CASES)
+def test_matvec_fp64(name, mode):
+    import torch
+    case = load(name)
+    prob, h, S = _problem(case, cache_level=mode)
+    D = int(case['D'])
+    for v, ref in zip(case['mv_in'], case['mv_out']):
+        x = torch.as_tensor(v[:D]).cuda()
+        y = prob.op.matvec(x).cpu().numpy()
+        np.testing.assert_allclose(y, ref[:D], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_matvec_fp32_error_bound(name):
+    """complex64 / float32 matvec: relative error <= 1e-6 against the FP64 reference output."""
+    import torch
+    case = load(name)
+    for mode in [(0, 0), (1, 0)]:
+        prob, h, S = _problem(case, cache_level=mode)
+        D = int(case['D'])
+        for v, ref in zip(case['mv_in'], case['mv_out']):
+            dt = torch.float32 if h.is_real else torch.complex64
+            x = torch.as_tensor(v[:D]).to(dt).cuda()
+            y = prob.op.matvec(x).cpu().numpy().astype(ref.dtype)
+            # error of the 32-bit product relative to the exact product of the rounded input
+            exact = prob.op.matvec(x.to(torch.float64 if h.is_real else torch.complex128))
+            e = np.linalg.norm(y - exact.cpu().numpy()) / np.linalg.norm(exact.cpu().numpy())
+            assert e <= 1e-6, e
+            e2 = np.linalg.norm(y - ref[:D]) / np.linalg.norm(ref[:D])
+            assert e2 <= 1e-6, e2
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_connectivity_matches_reference_table(name):
+    case = load(name)
+    prob, h, S = _problem(case, cache_level=(1, 0))
+    D = int(case['D'])
+    rowptr, col, grp = prob.op.connectivity()
+    xs = case['xsources'][:, :D]
+    dg = prob.terms.diag_group
+    exp_col, exp_grp, exp_ptr = [], [], [0]
+    for i in range(D):
+        for j in range(xs.shape[0]):
+            if j != dg and xs[j, i] >= 0:
+                exp_col.append(xs[j, i])
+                exp_grp.append(j)
+        exp_ptr.append(len(exp_col))
+    np.testing.assert_array_equal(rowptr, exp_ptr)
+    np.testing.assert_array_equal(col, exp_col)
+    np.testing.assert_array_equal(grp, exp_grp)
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_sqd_matches_reference(name):
+    from rqutils_gb300.sqd import sqd
+    case = load(name)
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        eig, vec, basis, info = sqd(hamiltonian(case), case['states'],
+                                    states_size=int(case['states_size']), return_info=True)
+    ref = float(case['eigval'])
+    np.testing.assert_array_equal(basis, case['basis'])
+    if np.isnan(ref):
+        assert np.isnan(eig) and info['niter'] == int(case['niter'])
+        return
+    assert abs(eig - ref) <= 1e-10 * max(1., abs(ref)), (eig, ref)
+    assert abs(np.vdot(case['eigvec'], vec)) > 1 - 1e-9
+    assert vec.dtype == case['eigvec'].dtype
+    # same algorithm and operation order up to reduction order: iteration counts agree closely
+    assert abs(info['niter'] - int(case['niter'])) <= max(2, int(0.05 * int(case['niter'])))
+
+
+@pytest.mark.parametrize('name', CONVERGING)
+@pytest.mark.parametrize('variant', ['reference', 'fast'])
+@pytest.mark.parametrize('cache_level', [(0, 0), (1, 2)])
+def test_sqd_modes_and_variants(name, variant, cache_level):
+    from rqutils_gb300.sqd import sqd
+    case = load(name)
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        eig = sqd(hamiltonian(case), case['states'], return_eigvec=False, variant=variant,
+                  cache_level=cache_level)
+    ref = float(case['eigval'])
+    assert abs(eig - ref) <= 1e-9 * max(1., abs(ref)), (eig, ref)
+
+
+@pytest.mark.parametrize('name', ['notebook', 'hubbard2x2', 'local12', 'n16dense'])
+def test_sqd_mixed_precision(name):
+    from rqutils_gb300.sqd import sqd
+    case = load(name)
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        eig, vec, _, info = sqd(hamiltonian(case), case['states'], precision='mixed',
+                                return_info=True)
+    ref = float(case['eigval'])
+    assert abs(eig - ref) <= 1e-8 * max(1., abs(ref)), (eig, ref, info)
+
+
+def test_fullspace_matmul():
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    case = load('fullspace')
+    h = PauliSumXZ.from_paulisum(([str(p) for p in case['paulis']], case['coeffs']))
+    out = h.matmul(case['rhs1'])
+    np.testing.assert_allclose(out, case['out1'], rtol=1e-12, atol=1e-12)
+    two = h.matmul(np.stack([case['rhs1'], 2 * case['rhs1']], axis=1))
+    np.testing.assert_allclose(two[:, 1], 2 * case['out1'], rtol=1e-12, atol=1e-12)
+
+
+def test_ground_locg_callable_and_matrix():
+    import torch
+    from rqutils_gb300.ground_locg import ground_locg
+    from oracle.ground_locg import ground_locg as oracle_locg
+    rng = np.random.default_rng(4)
+    a = rng.normal(size=(60, 60)) + 1j * rng.normal(size=(60, 60))
+    h = a + a.conj().T
+    x0 = np.zeros(60, complex)
+    x0[3] = 1
+    th_o, x_o, n_o = oracle_locg(lambda v: h @ v, x0)
+    th, x, n = ground_locg(h, x0)
+    assert abs(th - np.linalg.eigvalsh(h)[0]) < 1e-10
+    assert abs(th - th_o) < 1e-10 and abs(n - n_o) <= 2
+    ht = torch.as_tensor(h).cuda()
+    th2, x2, n2 = ground_locg(lambda v, s: s * (ht @ v), 3, args=(1.0,), vspace=(60, np.complex128))
+    assert abs(th2 - th) < 1e-10 and isinstance(x2, np.ndarray)
+
+
+def test_unsorted_subspace_rejected():
+    from rqutils_gb300.device import DeviceSubspace
+    from rqutils_gb300._lib import RqError
+    with pytest.raises(RqError, match='strictly increasing'):
+        DeviceSubspace(np.array([1, 5, 3], dtype=np.uint64), num_qubits=4)
+    with pytest.raises(RqError):
+        DeviceSubspace(np.array([1, 5, 5], dtype=np.uint64), num_qubits=4)
+
+
+def test_extreme_keys_and_empty_choice():
+    """States containing both 0 and 2^64-1 force the empty key into a gap."""
+    import torch
+    from rqutils_gb300.device import DeviceSubspace
+    S = np.array([0, 1, 2, 7, 2 ** 63, 2 ** 64 - 2, 2 ** 64 - 1], dtype=np.uint64)
+    sub = DeviceSubspace(S, num_qubits=64, filter_masks=(0, 0))
+    assert sub.c.empty_key == 3
+    xs = sub.xsource(np.array([0, 1, 2 ** 64 - 1, 5], dtype=np.uint64)).cpu().numpy()
+    from oracle.sqd import xsource_search
+    for j, x in enumerate([0, 1, 2 ** 64 - 1, 5]):
+        np.testing.assert_array_equal(xs[j], xsource_search(S, x))
