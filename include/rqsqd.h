@@ -56,7 +56,7 @@ extern "C" {
 #define RQ_E_RANGE       7   /* a size exceeds a fixed limit of the entry point           */
 
 /* lookup structures for S[i] ^ x membership */
-#define RQ_LOOKUP_HASH     0  /* bucketed open-addressing hash table (4 keys per 32-byte bucket) */
+#define RQ_LOOKUP_HASH     0  /* open addressing, buckets of 4 keys (uint32 or uint64)         */
 #define RQ_LOOKUP_BSEARCH  1  /* shared-memory sampled binary search over the sorted states      */
 #define RQ_LOOKUP_IDENTITY 2  /* full space: S[i] = i, D = 2^n (PauliSumXZ.matmul)               */
 
@@ -70,10 +70,12 @@ extern "C" {
 typedef struct rq_subspace {
     const uint64_t *states;  /* [D] strictly increasing                                   */
     int64_t   D;             /* subspace dimension, 1 <= D < 2^31                          */
-    uint64_t *hkeys;         /* [4 << hbits] hash keys (RQ_LOOKUP_HASH)                    */
-    int32_t  *hvals;         /* [4 << hbits] row index of each key                         */
+    void     *hkeys;         /* 2^hbits buckets of 4 keys: (key_bits / 2) << hbits bytes    */
+    int32_t  *hvals;         /* [4 << hbits] row index of each key slot                    */
     int32_t   hbits;         /* log2(number of buckets), from rq_subspace_sizes            */
     int32_t   lookup;        /* RQ_LOOKUP_*                                                */
+    int32_t   key_bits;      /* 32: states and every X mask < 2^32 (16-byte buckets); 64   */
+    int32_t   pad_;
     uint64_t  empty_key;     /* written by rq_subspace_build: a value not in states        */
     uint64_t  fmask_a;       /* sector filter masks (0, 0 = filter off)                    */
     uint64_t  fmask_b;
@@ -107,8 +109,9 @@ typedef struct rq_operator {
 
 /* ---- sizing (host only) ---------------------------------------------------------------- */
 
-/* Hash-table bucket count exponent for D states at load factor <= 1/2 (4 slots per bucket). */
-int rq_subspace_sizes(int64_t D, int32_t *hbits);
+/* Hash-table bucket count exponent for D states at load factor <= 1/8 (4 keys per bucket):
+ * hkeys takes (key_bits / 2) << hbits bytes, hvals 4 << hbits int32. */
+int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits);
 
 /* Bytes of scratch that rq_matvec / rq_conn_build / rq_dots need for their reductions/scans. */
 int rq_scratch_size(int64_t D, size_t *bytes);

@@ -24,6 +24,7 @@ _c_void_p = ctypes.c_void_p
 class Subspace(ctypes.Structure):
     _fields_ = [('states', _c_void_p), ('D', ctypes.c_int64), ('hkeys', _c_void_p),
                 ('hvals', _c_void_p), ('hbits', ctypes.c_int32), ('lookup', ctypes.c_int32),
+                ('key_bits', ctypes.c_int32), ('pad_', ctypes.c_int32),
                 ('empty_key', ctypes.c_uint64), ('fmask_a', ctypes.c_uint64),
                 ('fmask_b', ctypes.c_uint64), ('fbits', _c_void_p)]
 
@@ -61,7 +62,7 @@ class LobpcgResult(ctypes.Structure):
 # name -> (restype, argtypes); mirrors include/rqsqd.h
 _P = ctypes.POINTER
 SIGNATURES = {
-    'rq_subspace_sizes': (ctypes.c_int, [ctypes.c_int64, _P(ctypes.c_int32)]),
+    'rq_subspace_sizes': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int32)]),
     'rq_scratch_size': (ctypes.c_int, [ctypes.c_int64, _P(ctypes.c_size_t)]),
     'rq_subspace_build': (ctypes.c_int, [_P(Subspace), _c_void_p, _c_void_p]),
     'rq_xsource': (ctypes.c_int, [_P(Subspace), _c_void_p, ctypes.c_int32, _c_void_p, _c_void_p]),

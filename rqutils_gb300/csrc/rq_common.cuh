@@ -113,69 +113,139 @@ struct VT<double2> {
 // ------------------------------------------------------------------------------------------
 // hashing and lookups
 // ------------------------------------------------------------------------------------------
-__host__ __device__ __forceinline__ uint64_t mix64(uint64_t k) {
-    k ^= k >> 31;
-    k *= 0x7fb5d329728ea185ULL;
-    k ^= k >> 27;
-    k *= 0x81dadef4bc2dd44dULL;
-    k ^= k >> 33;
-    return k;
+// A bucket holds 4 keys: 16 bytes of uint32 keys when every state and X mask fits in 32 bits,
+// else 32 bytes of uint64 keys.  Slots of a bucket fill in order; a full bucket continues the
+// probe chain in the next bucket.  The table is sized for a load factor <= 1/8 (half a key per
+// bucket on average), so a bucket is full with probability ~0.2% and nearly every lookup is one
+// load.
+//
+// The bucket index comes from a GF(2)-linear hash h(k) = XOR of R[i] over the set bits i of k,
+// with fixed pseudo-random 32-bit words R[i].  Linearity gives h(s ^ x) = h(s) ^ h(x): a row
+// hashes its state once and each X group contributes one XOR.  h is evaluated with per-byte
+// tables T[b][v] = h(v << 8b) kept in shared memory.
+__host__ __device__ constexpr uint32_t lin_word(int i) {
+    uint32_t h = (uint32_t)(i + 1) * 0x9E3779B9u;
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
 }
 
-__device__ __forceinline__ uint64_t bucket_of(uint64_t key, int hbits) {
-    return mix64(key) >> (64 - hbits);
+constexpr int kHashTableWords = 8 * 256;  // shared-memory words for 64-bit keys
+constexpr int kBucketSlots = 4;
+
+// Fill T[b * 256 + v] for b < nbytes (all threads of the block; caller synchronises).
+__device__ inline void init_hash_tables(uint32_t *T, int nbytes) {
+    for (int idx = threadIdx.x; idx < nbytes * 256; idx += blockDim.x) {
+        const int b = idx >> 8, v = idx & 255;
+        uint32_t h = 0;
+#pragma unroll
+        for (int bit = 0; bit < 8; ++bit)
+            if ((v >> bit) & 1) h ^= lin_word(8 * b + bit);
+        T[idx] = h;
+    }
 }
 
-// One 32-byte bucket (4 keys) in a single 256-bit read-only load.
-__device__ __forceinline__ void load_bucket(const uint64_t *p, uint64_t &k0, uint64_t &k1,
-                                            uint64_t &k2, uint64_t &k3) {
-    asm volatile("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];"
-                 : "=l"(k0), "=l"(k1), "=l"(k2), "=l"(k3)
-                 : "l"(p));
+__device__ __forceinline__ uint32_t lin_hash(const uint32_t *T, uint64_t k, int nbytes) {
+    uint32_t h = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+        if (b < nbytes) h ^= T[(b << 8) | (uint32_t)((k >> (8 * b)) & 255u)];
+    return h;
 }
 
-// Slot of `t` among the four keys, -1 when absent; `open` is set when the bucket still has an
-// empty slot (slots fill in order, so an empty last slot ends the probe chain).
-__device__ __forceinline__ int match_bucket(uint64_t t, uint64_t empty, uint64_t k0, uint64_t k1,
-                                            uint64_t k2, uint64_t k3, bool &open) {
-    open = (k3 == empty);
-    if (k0 == t) return 0;
-    if (k1 == t) return 1;
-    if (k2 == t) return 2;
-    if (k3 == t) return 3;
+__device__ __forceinline__ uint32_t bucket_from_hash(uint32_t h, int hbits) {
+    return h >> (32 - hbits);
+}
+
+template <int KB>
+struct KeyWidth;
+template <>
+struct KeyWidth<64> {
+    using K = uint64_t;
+    static constexpr int kNbytes = 8;
+    static constexpr int kBucketBytes = 32;
+    struct Bucket { uint64_t k[4]; };
+    // one 32-byte bucket in a single 256-bit read-only load; `fill` when pred is false
+    static __device__ __forceinline__ Bucket load(const void *p, bool pred, uint64_t fill) {
+        Bucket b;
+        b.k[0] = b.k[1] = b.k[2] = b.k[3] = fill;
+        asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %5, 0;\n\t"
+            "@q ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];\n\t}"
+            : "+l"(b.k[0]), "+l"(b.k[1]), "+l"(b.k[2]), "+l"(b.k[3])
+            : "l"(p), "r"((unsigned)pred));
+        return b;
+    }
+};
+template <>
+struct KeyWidth<32> {
+    using K = uint32_t;
+    static constexpr int kNbytes = 4;
+    static constexpr int kBucketBytes = 16;
+    struct Bucket { uint32_t k[4]; };
+    static __device__ __forceinline__ Bucket load(const void *p, bool pred, uint64_t fill) {
+        Bucket b;
+        b.k[0] = b.k[1] = b.k[2] = b.k[3] = (uint32_t)fill;
+        asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %5, 0;\n\t"
+            "@q ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];\n\t}"
+            : "+r"(b.k[0]), "+r"(b.k[1]), "+r"(b.k[2]), "+r"(b.k[3])
+            : "l"(p), "r"((unsigned)pred));
+        return b;
+    }
+};
+
+// Branch-free bucket test: `any` when a slot equals t, `open` when the last slot is empty.
+template <typename Bk, typename K>
+__device__ __forceinline__ void test_bucket(const Bk &b, K t, K e, bool &any, bool &open) {
+    any = (b.k[0] == t) | (b.k[1] == t) | (b.k[2] == t) | (b.k[3] == t);
+    open = (b.k[3] == e);
+}
+
+template <typename Bk, typename K>
+__device__ __forceinline__ int slot_of(const Bk &b, K t) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (b.k[i] == t) return i;
     return -1;
 }
 
-// Continue a probe chain after a full bucket (rare at load factor <= 1/2).  Bounded by the
-// table size; a chain that never ends reports a miss and sets the error flag.
-static __device__ __noinline__ int probe_rest(const rq_subspace_t &S, uint64_t t, uint64_t b,
-                                       int *err) {
-    const uint64_t mask = (1ULL << S.hbits) - 1;
-    for (uint64_t n = 0; n <= mask; ++n) {
+template <int KB>
+__device__ __forceinline__ const void *bucket_ptr(const rq_subspace_t &S, uint32_t b) {
+    return static_cast<const unsigned char *>(S.hkeys) + (size_t)b * KeyWidth<KB>::kBucketBytes;
+}
+
+// Continue a probe chain after a full bucket, bounded by the table size; a chain that never ends
+// reports a miss and sets the error flag.
+template <int KB>
+static __device__ __noinline__ int probe_rest(const rq_subspace_t &S, uint64_t t, uint32_t b,
+                                              int *err) {
+    using K = typename KeyWidth<KB>::K;
+    const uint32_t mask = (1u << S.hbits) - 1u;
+    for (uint32_t n = 0; n <= mask; ++n) {
         b = (b + 1) & mask;
-        uint64_t k0, k1, k2, k3;
-        load_bucket(S.hkeys + (b << 2), k0, k1, k2, k3);
-        bool open;
-        int s = match_bucket(t, S.empty_key, k0, k1, k2, k3, open);
-        if (s >= 0) return S.hvals[(b << 2) + s];
-        if (open) return -1;
+        const auto bk = KeyWidth<KB>::load(bucket_ptr<KB>(S, b), true, S.empty_key);
+        const int s = slot_of(bk, (K)t);
+        if (s >= 0) return S.hvals[(size_t)b * kBucketSlots + s];
+        if (bk.k[3] == (K)S.empty_key) return -1;
     }
     if (err) atomicExch(err, RQ_E_TABLE);
     return -1;
 }
 
-// The empty key is not a state, so a target equal to it is a miss (it would otherwise match an
-// empty slot, whose row index is undefined).
-__device__ __forceinline__ int lookup_hash(const rq_subspace_t &S, uint64_t t, int *err) {
+// Full lookup of t starting at bucket b.  The empty key is not a state, so a target equal to it
+// is a miss (it would otherwise match an empty slot, whose row index is undefined).
+template <int KB>
+__device__ __forceinline__ int lookup_hash_at(const rq_subspace_t &S, uint64_t t, uint32_t b,
+                                              int *err) {
+    using K = typename KeyWidth<KB>::K;
     if (t == S.empty_key) return -1;
-    const uint64_t b = bucket_of(t, S.hbits);
-    uint64_t k0, k1, k2, k3;
-    load_bucket(S.hkeys + (b << 2), k0, k1, k2, k3);
-    bool open;
-    int s = match_bucket(t, S.empty_key, k0, k1, k2, k3, open);
-    if (s >= 0) return S.hvals[(b << 2) + s];
-    if (open) return -1;
-    return probe_rest(S, t, b, err);
+    const auto bk = KeyWidth<KB>::load(bucket_ptr<KB>(S, b), true, S.empty_key);
+    const int s = slot_of(bk, (K)t);
+    if (s >= 0) return S.hvals[(size_t)b * kBucketSlots + s];
+    if (bk.k[3] == (K)S.empty_key) return -1;
+    return probe_rest<KB>(S, t, b, err);
 }
 
 // Sampled binary search: `samp` (shared memory) holds states[(k * D) / ns] for k < ns.  The
@@ -201,6 +271,20 @@ __device__ __forceinline__ int lookup_bsearch(const rq_subspace_t &S, const uint
 // Sector filter: bit (popcount(t & a) * 65 + popcount(t & b)) of the 65 x 65 table.
 __device__ __forceinline__ bool sector_ok(const uint32_t *fb, uint64_t a, uint64_t b, uint64_t t) {
     const int bit = __popcll(t & a) * 65 + __popcll(t & b);
+    return (fb[bit >> 5] >> (bit & 31)) & 1u;
+}
+
+template <typename K>
+__device__ __forceinline__ bool sector_ok_k(const uint32_t *fb, K a, K b, K t) {
+    int pa, pb;
+    if (sizeof(K) == 8) {
+        pa = __popcll((unsigned long long)(t & a));
+        pb = __popcll((unsigned long long)(t & b));
+    } else {
+        pa = __popc((unsigned)(t & a));
+        pb = __popc((unsigned)(t & b));
+    }
+    const int bit = pa * 65 + pb;
     return (fb[bit >> 5] >> (bit & 31)) & 1u;
 }
 

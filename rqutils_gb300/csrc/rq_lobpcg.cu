@@ -506,19 +506,22 @@ __global__ void k_check(State *st) {
     st->axnorm = an;
     st->iter += 1;
     ++st->since_refresh;
-    bool conv = rn < st->tol * ((an - th) * st->tol_dim * 10.);
-    if (st->target_rel > 0. && rn <= st->target_rel * fabs(th)) conv = true;
-    if (!isfinite(rn) || !isfinite(th)) st->status = RQ_E_NONFINITE;
+    bool conv;
     if (st->phase_lo) {
-        // 32-bit phase: hand over once the residual is small or stops improving
-        if (rn < st->switch_rel * fabs(th)) conv = true;
+        // 32-bit phase: hand over once the residual is small or stops improving (the reference
+        // test with the 32-bit epsilon times the dimension is meaningless for large D)
+        conv = rn < st->switch_rel * fabs(th);
         if (rn < 0.7 * st->best_r) {
             st->best_r = rn;
             st->stall = 0;
         } else if (++st->stall >= 30) {
             conv = true;
         }
+    } else {
+        conv = rn < st->tol * ((an - th) * st->tol_dim * 10.);
+        if (st->target_rel > 0. && rn <= st->target_rel * fabs(th)) conv = true;
     }
+    if (!isfinite(rn) || !isfinite(th)) st->status = RQ_E_NONFINITE;
     if (st->variant == RQ_LOBPCG_FAST) {
         // carried products: confirm with fresh A x, A y before accepting
         if (conv && !st->certify) {

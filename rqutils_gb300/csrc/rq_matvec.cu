@@ -27,6 +27,8 @@ constexpr int kFilterBytes = 544;
 template <typename R>
 struct Tile {
     uint64_t *xm;
+    uint32_t *hx;  // linear hash of each X mask (hash-lookup kernel only)
+    uint2 *gs;     // (low 32 bits of the X mask, its hash): one 8-byte read per group
     int32_t *off;
     uint64_t *zm;
     cx<R> *cf;
@@ -36,14 +38,18 @@ __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(
 
 template <typename R>
 __host__ __device__ inline size_t tile_bytes(int gt, int kt) {
-    return align16((size_t)gt * 8) + align16((size_t)(gt + 1) * 4) + align16((size_t)kt * 8) +
-           (size_t)kt * sizeof(cx<R>);
+    return align16((size_t)gt * 8) + align16((size_t)gt * 4) + align16((size_t)gt * 8) +
+           align16((size_t)(gt + 1) * 4) + align16((size_t)kt * 8) + (size_t)kt * sizeof(cx<R>);
 }
 
 template <typename R>
 __device__ inline Tile<R> carve(unsigned char *p, int gt, int kt) {
     Tile<R> t;
     t.xm = reinterpret_cast<uint64_t *>(p);
+    p += align16((size_t)gt * 8);
+    t.hx = reinterpret_cast<uint32_t *>(p);
+    p += align16((size_t)gt * 4);
+    t.gs = reinterpret_cast<uint2 *>(p);
     p += align16((size_t)gt * 8);
     t.off = reinterpret_cast<int32_t *>(p);
     p += align16((size_t)(gt + 1) * 4);
@@ -54,11 +60,12 @@ __device__ inline Tile<R> carve(unsigned char *p, int gt, int kt) {
 }
 
 // Stage groups [g0, g1) into shared memory, g1 as large as the tile allows.  Returns g1, or -1
-// when group g0 alone exceeds the tile.  Every thread of the block must call it.
+// when group g0 alone exceeds the tile.  Every thread of the block must call it.  With a hash
+// table T the linear hash of each X mask is stored too.
 template <typename R>
 __device__ int load_tile(const rq_terms_t &T, int g0, int gt, int kt, const Tile<R> &tl,
-                         int *s_g1) {
-    __syncthreads();  // previous tile no longer in use
+                         int *s_g1, const uint32_t *htab = nullptr, int nbytes = 8) {
+    __syncthreads();  // previous tile no longer in use; tables written before are visible
     if (threadIdx.x == 0) *s_g1 = g0;
     __syncthreads();
     const int base = T.toff[g0];
@@ -70,7 +77,15 @@ __device__ int load_tile(const rq_terms_t &T, int g0, int gt, int kt, const Tile
     if (g1 == g0) return -1;
     const int ng = g1 - g0;
     const int nk = T.toff[g1] - base;
-    for (int g = threadIdx.x; g < ng; g += blockDim.x) tl.xm[g] = T.xmask[g0 + g];
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const uint64_t xv = T.xmask[g0 + g];
+        tl.xm[g] = xv;
+        if (htab) {
+            const uint32_t h = lin_hash(htab, xv, nbytes);
+            tl.hx[g] = h;
+            tl.gs[g] = make_uint2((uint32_t)xv, h);
+        }
+    }
     for (int g = threadIdx.x; g <= ng; g += blockDim.x) tl.off[g] = T.toff[g0 + g] - base;
     for (int k = threadIdx.x; k < nk; k += blockDim.x) {
         tl.zm[k] = T.zmask[base + k];
@@ -95,41 +110,14 @@ __device__ __forceinline__ void add_group(const cx<R> *cf, const uint64_t *zm, i
     acc.add(cmul(d.get(), xv));
 }
 
-// Visit the hits of row state s over groups [g0, g1) (xm indexed by g - g0), skipping `skip`.
-// on_hit(g, m) is called in ascending g.
-template <int LK, typename F>
+// Visit the hits of row state s over groups [g0, g1) (xm indexed by g - g0), skipping `skip`,
+// calling on_hit(g, m) in ascending g.  Hash lookups hash each target in full (T: tables).
+template <int LK, int KB, typename F>
 __device__ __forceinline__ void for_hits(const rq_subspace_t &S, const uint32_t *fb,
-                                         const uint64_t *samp, int ns, const uint64_t *xm, int g0,
-                                         int g1, int skip, uint64_t s, int *err, F &&on_hit) {
-    int g = g0;
-    if (LK == RQ_LOOKUP_HASH) {
-        for (; g + 4 <= g1; g += 4) {
-            uint64_t t[4], b[4], k0[4], k1[4], k2[4], k3[4];
-            bool q[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                t[u] = s ^ xm[g + u - g0];
-                q[u] = (g + u != skip) && (t[u] != S.empty_key) &&
-                       sector_ok(fb, S.fmask_a, S.fmask_b, t[u]);
-                b[u] = bucket_of(t[u], S.hbits);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (q[u]) load_bucket(S.hkeys + (b[u] << 2), k0[u], k1[u], k2[u], k3[u]);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (!q[u]) continue;
-                bool open;
-                const int sl = match_bucket(t[u], S.empty_key, k0[u], k1[u], k2[u], k3[u], open);
-                int m;
-                if (sl >= 0) m = __ldg(S.hvals + (b[u] << 2) + sl);
-                else if (open) m = -1;
-                else m = probe_rest(S, t[u], b[u], err);
-                if (m >= 0) on_hit(g + u, (int64_t)m);
-            }
-        }
-    }
-    for (; g < g1; ++g) {
+                                         const uint64_t *samp, int ns, const uint32_t *T,
+                                         const uint64_t *xm, int g0, int g1, int skip, uint64_t s,
+                                         int *err, F &&on_hit) {
+    for (int g = g0; g < g1; ++g) {
         if (g == skip) continue;
         const uint64_t t = s ^ xm[g - g0];
         int64_t m;
@@ -137,7 +125,13 @@ __device__ __forceinline__ void for_hits(const rq_subspace_t &S, const uint32_t 
             m = (t < (uint64_t)S.D) ? (int64_t)t : -1;
         } else {
             if (!sector_ok(fb, S.fmask_a, S.fmask_b, t)) continue;
-            m = (LK == RQ_LOOKUP_HASH) ? lookup_hash(S, t, err) : lookup_bsearch(S, samp, ns, t);
+            if (LK == RQ_LOOKUP_HASH) {
+                if (KB == 32 && (t >> 32) != 0) continue;
+                m = lookup_hash_at<KB>(
+                    S, t, bucket_from_hash(lin_hash(T, t, KeyWidth<KB>::kNbytes), S.hbits), err);
+            } else {
+                m = lookup_bsearch(S, samp, ns, t);
+            }
         }
         if (m >= 0) on_hit(g, m);
     }
@@ -154,7 +148,137 @@ __device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, ui
 }
 
 // ------------------------------------------------------------------------------------------
-// FREE mode
+// FREE mode with the hash table: the hot kernel
+// ------------------------------------------------------------------------------------------
+// Per row: h(s) once; per group: t = s ^ x_j, sector filter, bucket = (h(s) ^ h(x_j)) >> shift,
+// one 32-byte bucket load.  Four groups are processed per step with their bucket loads issued
+// together.  Keys and the row state use KB-bit arithmetic.
+template <typename V, int KB, bool FILTER>
+__global__ void __launch_bounds__(kThreads, 3)
+k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int gt, int kt,
+              int *err, const int *gate, const int *gate2) {
+    using R = typename VT<V>::R;
+    using K = typename KeyWidth<KB>::K;
+    constexpr int NB = KeyWidth<KB>::kNbytes;
+    constexpr int kBucketBytes = KeyWidth<KB>::kBucketBytes;
+    constexpr int U = (KB == 32) ? 8 : 4;  // probes in flight per thread
+    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_g1;
+    const rq_subspace_t &S = op.sub;
+    const rq_terms_t &T = op.terms;
+    uint32_t *fb = reinterpret_cast<uint32_t *>(smem);
+    uint32_t *htab = reinterpret_cast<uint32_t *>(smem + kFilterBytes);
+    const Tile<R> tl = carve<R>(smem + kFilterBytes + NB * 256 * 4, gt, kt);
+    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) fb[w] = S.fbits[w];
+    init_hash_tables(htab, NB);
+
+    const int64_t D = S.D;
+    const bool d0 = (op.diag0 != nullptr) && (T.diag_group >= 0);
+    const int gstart = (d0 && T.diag_group == 0) ? 1 : 0;
+    const int skip = T.diag_group;
+    const K fa = (K)S.fmask_a, fbm = (K)S.fmask_b, empty = (K)S.empty_key;
+    const int shift = 32 - S.hbits;
+    const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
+    int g1_first = (gstart < T.J) ? load_tile<R>(T, gstart, gt, kt, tl, &s_g1, htab, NB) : T.J;
+    if (g1_first < 0) {
+        if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
+        return;
+    }
+    __syncthreads();  // tables visible even when no tile was loaded
+    const bool resident = (g1_first >= T.J);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < D;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const bool active = i < D;
+        const uint64_t s64 = active ? __ldg(S.states + i) : 0ULL;
+        const K s = (K)s64;
+        const uint32_t hs = lin_hash(htab, s64, NB);
+        CAcc<R> acc;
+        if (active && d0) {
+            const R dv = (R)op.diag0[i];
+            const cx<R> xv = VT<V>::ld(x, i);
+            acc.add({dv * xv.re, dv * xv.im});
+        }
+        if (!resident && base != (int64_t)blockIdx.x * blockDim.x)
+            g1_first = load_tile<R>(T, gstart, gt, kt, tl, &s_g1, htab, NB);
+        int g0 = gstart, g1 = g1_first;
+        while (g0 < T.J) {
+            if (g1 < 0) {
+                if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
+                return;  // uniform across the block
+            }
+            if (active) {
+                if (!d0 && skip >= g0 && skip < g1)
+                    add_group<R>(tl.cf, tl.zm, tl.off[skip - g0], tl.off[skip - g0 + 1], s64,
+                                 VT<V>::ld(x, i), true, acc);
+                int g = g0;
+                for (; g + U <= g1; g += U) {
+                    K t[U];
+                    uint32_t b[U];
+                    bool q[U];
+                    typename KeyWidth<KB>::Bucket w[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const int gl = g + u - g0;
+                        uint32_t hxg;
+                        if (KB == 32) {
+                            const uint2 e = tl.gs[gl];
+                            t[u] = s ^ (K)e.x;
+                            hxg = e.y;
+                        } else {
+                            t[u] = s ^ (K)tl.xm[gl];
+                            hxg = tl.hx[gl];
+                        }
+                        q[u] = (g + u != skip);
+                        if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
+                        b[u] = (hs ^ hxg) >> shift;
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+                        w[u] = KeyWidth<KB>::load(keys + (size_t)b[u] * kBucketBytes, q[u],
+                                                  S.empty_key);
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        bool any, open;
+                        test_bucket(w[u], t[u], empty, any, open);
+                        // rare: a hit, a full bucket, or a target equal to the empty key
+                        if (q[u] && (any || !open)) {
+                            int m = -1;
+                            if (t[u] != empty) {
+                                const int sl = slot_of(w[u], t[u]);
+                                if (sl >= 0) m = __ldg(S.hvals + (size_t)b[u] * kBucketSlots + sl);
+                                else if (!open) m = probe_rest<KB>(S, (uint64_t)t[u], b[u], err);
+                            }
+                            if (m >= 0) {
+                                const int gl = g + u - g0;
+                                add_group<R>(tl.cf, tl.zm, tl.off[gl], tl.off[gl + 1], s64,
+                                             VT<V>::ld(x, m), true, acc);
+                            }
+                        }
+                    }
+                }
+                for (; g < g1; ++g) {
+                    if (g == skip) continue;
+                    const int gl = g - g0;
+                    const K t = s ^ (K)tl.xm[gl];
+                    if (t == empty || (FILTER && !sector_ok_k<K>(fb, fa, fbm, t))) continue;
+                    const int m = lookup_hash_at<KB>(S, (uint64_t)t, (hs ^ tl.hx[gl]) >> shift, err);
+                    if (m >= 0)
+                        add_group<R>(tl.cf, tl.zm, tl.off[gl], tl.off[gl + 1], s64, VT<V>::ld(x, m),
+                                     true, acc);
+                }
+            }
+            if (g1 >= T.J) break;
+            g0 = g1;
+            g1 = load_tile<R>(T, g0, gt, kt, tl, &s_g1, htab, NB);
+        }
+        if (active) VT<V>::st(y, i, acc.get());
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// FREE mode, generic lookups (sampled binary search; identity for the full space)
 // ------------------------------------------------------------------------------------------
 template <typename V, int LK>
 __global__ void __launch_bounds__(kThreads)
@@ -182,6 +306,7 @@ k_matvec_free(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
         if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
         return;
     }
+    __syncthreads();
     const bool resident = (g1_first >= T.J);
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < D;
          base += (int64_t)gridDim.x * blockDim.x) {
@@ -207,11 +332,11 @@ k_matvec_free(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
                 if (!d0 && skip >= g0 && skip < g1)
                     add_group<R>(tl.cf, tl.zm, tl.off[skip - g0], tl.off[skip - g0 + 1], s,
                                  VT<V>::ld(x, i), stop_at_zero, acc);
-                for_hits<LK>(S, fb, samp, ns, tl.xm, g0, g1, skip, s, err,
-                             [&](int g, int64_t m) {
-                                 add_group<R>(tl.cf, tl.zm, tl.off[g - g0], tl.off[g - g0 + 1],
-                                              s, VT<V>::ld(x, m), stop_at_zero, acc);
-                             });
+                for_hits<LK, 64>(S, fb, samp, ns, nullptr, tl.xm, g0, g1, skip, s, err,
+                                 [&](int g, int64_t m) {
+                                     add_group<R>(tl.cf, tl.zm, tl.off[g - g0], tl.off[g - g0 + 1],
+                                                  s, VT<V>::ld(x, m), stop_at_zero, acc);
+                                 });
             }
             if (g1 >= T.J) break;
             g0 = g1;
@@ -224,20 +349,22 @@ k_matvec_free(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
 // ------------------------------------------------------------------------------------------
 // connectivity cache
 // ------------------------------------------------------------------------------------------
-template <int LK>
+template <int LK, int KB>
 __global__ void __launch_bounds__(kThreads)
 k_conn_count(const rq_operator_t op, int64_t *__restrict__ rowcnt, int *err) {
     __shared__ uint32_t fb[RQ_FILTER_WORDS];
     __shared__ uint64_t samp[LK == RQ_LOOKUP_BSEARCH ? kSample : 1];
+    __shared__ uint32_t T[LK == RQ_LOOKUP_HASH ? kHashTableWords : 1];
     const rq_subspace_t &S = op.sub;
     const int ns = (LK == RQ_LOOKUP_BSEARCH) ? (int)(S.D < kSample ? S.D : kSample) : 0;
     load_lookup_smem<LK>(S, fb, samp, ns);
+    if (LK == RQ_LOOKUP_HASH) init_hash_tables(T, KeyWidth<KB>::kNbytes);
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.D;
          i += (int64_t)gridDim.x * blockDim.x) {
         int64_t c = 0;
-        for_hits<LK>(S, fb, samp, ns, op.terms.xmask, 0, op.terms.J, op.terms.diag_group,
-                     __ldg(S.states + i), err, [&](int, int64_t) { ++c; });
+        for_hits<LK, KB>(S, fb, samp, ns, T, op.terms.xmask, 0, op.terms.J, op.terms.diag_group,
+                         __ldg(S.states + i), err, [&](int, int64_t) { ++c; });
         rowcnt[i] = c;
     }
 }
@@ -256,22 +383,24 @@ __device__ __forceinline__ cx<R> group_diag(const rq_terms_t &T, int g, uint64_t
     return d.get();
 }
 
-template <typename V, int LK>
+template <typename V, int LK, int KB>
 __global__ void __launch_bounds__(kThreads)
 k_conn_fill(const rq_operator_t op, const int64_t *__restrict__ rowptr, int32_t *__restrict__ col,
             int32_t *__restrict__ grp, V *__restrict__ val, int *err) {
     using R = typename VT<V>::R;
     __shared__ uint32_t fb[RQ_FILTER_WORDS];
     __shared__ uint64_t samp[LK == RQ_LOOKUP_BSEARCH ? kSample : 1];
+    __shared__ uint32_t T[LK == RQ_LOOKUP_HASH ? kHashTableWords : 1];
     const rq_subspace_t &S = op.sub;
     const int ns = (LK == RQ_LOOKUP_BSEARCH) ? (int)(S.D < kSample ? S.D : kSample) : 0;
     load_lookup_smem<LK>(S, fb, samp, ns);
+    if (LK == RQ_LOOKUP_HASH) init_hash_tables(T, KeyWidth<KB>::kNbytes);
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.D;
          i += (int64_t)gridDim.x * blockDim.x) {
         int64_t p = rowptr[i];
         const uint64_t s = __ldg(S.states + i);
-        for_hits<LK>(S, fb, samp, ns, op.terms.xmask, 0, op.terms.J, op.terms.diag_group, s, err,
+        for_hits<LK, KB>(S, fb, samp, ns, T, op.terms.xmask, 0, op.terms.J, op.terms.diag_group, s, err,
                      [&](int g, int64_t m) {
                          col[p] = (int32_t)m;
                          if (grp) grp[p] = g;
@@ -437,6 +566,48 @@ int launch_csr(const rq_operator_t &op, const void *x, void *y, cudaStream_t st,
 // ------------------------------------------------------------------------------------------
 // host dispatch
 // ------------------------------------------------------------------------------------------
+// Dynamic shared memory, opt-in above 48 KB and cached occupancy for one kernel instantiation.
+// The occupancy query is cached per instantiation and size (it is also reached while a stream is
+// being captured, where only stream work should be issued).
+template <typename KernT>
+int prepare_launch(KernT kern, size_t smem, size_t &configured, size_t &occ_smem, int &occ_blocks,
+                   int64_t D, int &grid) {
+    if (smem > 48 * 1024 && smem > configured) {
+        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    if (occ_smem != smem) {
+        int per = 0;
+        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, smem));
+        occ_blocks = per < 1 ? 1 : per;
+        occ_smem = smem;
+    }
+    int64_t g = (D + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)sm_count() * occ_blocks;
+    if (g > cap) g = cap;
+    grid = (int)(g < 1 ? 1 : g);
+    return RQ_OK;
+}
+
+template <typename V, int KB, bool FILTER>
+int launch_hash(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
+                const int *gate, const int *gate2) {
+    using R = typename VT<V>::R;
+    const rq_terms_t &T = op.terms;
+    const int gt = T.J < kGT ? (T.J > 0 ? T.J : 1) : kGT;
+    const int kt = T.K < kKT ? (T.K > 0 ? T.K : 1) : kKT;
+    const size_t smem = kFilterBytes + KeyWidth<KB>::kNbytes * 256 * 4 + tile_bytes<R>(gt, kt);
+    auto kern = k_matvec_hash<V, KB, FILTER>;
+    static size_t configured = 0, occ_smem = ~size_t(0);
+    static int occ_blocks = 1;
+    int grid = 1;
+    RQ_TRY(prepare_launch(kern, smem, configured, occ_smem, occ_blocks, op.sub.D, grid));
+    kern<<<grid, kThreads, smem, st>>>(op, static_cast<const V *>(x), static_cast<V *>(y), gt, kt,
+                                       err, gate, gate2);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}
+
 template <typename V, int LK>
 int launch_free(const rq_operator_t &op, const void *x, void *y, int stop_at_zero, int *err,
                 cudaStream_t st, const int *gate = nullptr, const int *gate2 = nullptr) {
@@ -484,8 +655,15 @@ int matvec_typed(const rq_operator_t &op, const void *x, void *y, void *scratch,
     int *err = scratch ? scratch_err(scratch) : nullptr;
     switch (op.mode) {
         case RQ_MODE_FREE:
-            if (op.sub.lookup == RQ_LOOKUP_HASH)
-                return launch_free<V, RQ_LOOKUP_HASH>(op, x, y, 1, err, st, gate, gate2);
+            if (op.sub.lookup == RQ_LOOKUP_HASH) {
+                // the sector filter is off when both masks are zero
+                const bool filt = (op.sub.fmask_a | op.sub.fmask_b) != 0;
+                if (op.sub.key_bits == 32)
+                    return filt ? launch_hash<V, 32, true>(op, x, y, err, st, gate, gate2)
+                                : launch_hash<V, 32, false>(op, x, y, err, st, gate, gate2);
+                return filt ? launch_hash<V, 64, true>(op, x, y, err, st, gate, gate2)
+                            : launch_hash<V, 64, false>(op, x, y, err, st, gate, gate2);
+            }
             if (op.sub.lookup == RQ_LOOKUP_BSEARCH)
                 return launch_free<V, RQ_LOOKUP_BSEARCH>(op, x, y, 1, err, st, gate, gate2);
             return fail(RQ_E_ARG, "rq_matvec: unsupported lookup for a subspace");
@@ -583,10 +761,12 @@ RQ_API int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col,
     if (!col) {
         RQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
         RQ_CUDA(cudaMemsetAsync(rowptr, 0, sizeof(int64_t), st));
-        if (S.lookup == RQ_LOOKUP_HASH)
-            k_conn_count<RQ_LOOKUP_HASH><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
+        if (S.lookup == RQ_LOOKUP_HASH && S.key_bits == 32)
+            k_conn_count<RQ_LOOKUP_HASH, 32><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
+        else if (S.lookup == RQ_LOOKUP_HASH)
+            k_conn_count<RQ_LOOKUP_HASH, 64><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
         else
-            k_conn_count<RQ_LOOKUP_BSEARCH><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
+            k_conn_count<RQ_LOOKUP_BSEARCH, 64><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
         RQ_CUDA(cudaGetLastError());
         const int64_t nb = (D + 1023) / 1024;
         int64_t *bsum = scratch_scan(scratch);
@@ -604,12 +784,15 @@ RQ_API int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col,
     const int g = grid_rows(D);
 #define RQ_FILL(V)                                                                                  \
     do {                                                                                            \
-        if (S.lookup == RQ_LOOKUP_HASH)                                                             \
-            k_conn_fill<V, RQ_LOOKUP_HASH><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,           \
-                                                                   static_cast<V *>(val), err);     \
+        if (S.lookup == RQ_LOOKUP_HASH && S.key_bits == 32)                                         \
+            k_conn_fill<V, RQ_LOOKUP_HASH, 32><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,       \
+                                                                       static_cast<V *>(val), err); \
+        else if (S.lookup == RQ_LOOKUP_HASH)                                                        \
+            k_conn_fill<V, RQ_LOOKUP_HASH, 64><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,       \
+                                                                       static_cast<V *>(val), err); \
         else                                                                                        \
-            k_conn_fill<V, RQ_LOOKUP_BSEARCH><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,        \
-                                                                      static_cast<V *>(val), err);  \
+            k_conn_fill<V, RQ_LOOKUP_BSEARCH, 64><<<g, kThreads, 0, st>>>(*op, rowptr, col, grp,    \
+                                                                          static_cast<V *>(val), err); \
     } while (0)
     switch (val ? vtype : RQ_C128) {
         case RQ_F32: RQ_FILL(float); break;

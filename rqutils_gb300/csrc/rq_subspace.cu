@@ -28,20 +28,34 @@ __global__ void k_fill_u64(uint64_t *p, int64_t n, uint64_t v) {
 // Insert every state into its bucket chain: claim the first empty slot with a CAS.  Keys are
 // distinct, so a failed CAS always means "occupied by another key".  Slots of a bucket are
 // claimed in order, which keeps the occupied slots a prefix of the bucket.
-__global__ void k_hash_insert(const uint64_t *__restrict__ states, int64_t D,
-                              unsigned long long *keys, int32_t *vals, int hbits,
-                              unsigned long long empty, int *err) {
-    const uint64_t mask = (1ULL << hbits) - 1;
+template <int KB>
+__global__ void __launch_bounds__(kThreads)
+k_hash_insert(const uint64_t *__restrict__ states, int64_t D, void *keys, int32_t *vals, int hbits,
+              uint64_t empty, int *err) {
+    __shared__ uint32_t T[kHashTableWords];
+    init_hash_tables(T, KeyWidth<KB>::kNbytes);
+    __syncthreads();
+    constexpr int kSlots = kBucketSlots;
+    const uint32_t mask = (1u << hbits) - 1u;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned long long key = states[i];
-        uint64_t b = bucket_of(key, hbits);
+        const uint64_t key = states[i];
+        uint32_t b = bucket_from_hash(lin_hash(T, key, KeyWidth<KB>::kNbytes), hbits);
         bool done = false;
-        for (uint64_t n = 0; n <= mask && !done; ++n) {
-            unsigned long long *slot = keys + (b << 2);
-            for (int s = 0; s < 4; ++s) {
-                if (atomicCAS(slot + s, empty, key) == empty) {
-                    vals[(b << 2) + s] = (int32_t)i;
+        for (uint32_t n = 0; n <= mask && !done; ++n) {
+            for (int s = 0; s < kSlots; ++s) {
+                const size_t slot = (size_t)b * kSlots + s;
+                bool won;
+                if (KB == 64) {
+                    unsigned long long *p = static_cast<unsigned long long *>(keys) + slot;
+                    won = atomicCAS(p, (unsigned long long)empty, (unsigned long long)key) ==
+                          (unsigned long long)empty;
+                } else {
+                    unsigned int *p = static_cast<unsigned int *>(keys) + slot;
+                    won = atomicCAS(p, (unsigned int)empty, (unsigned int)key) == (unsigned int)empty;
+                }
+                if (won) {
+                    vals[slot] = (int32_t)i;
                     done = true;
                     break;
                 }
@@ -50,6 +64,12 @@ __global__ void k_hash_insert(const uint64_t *__restrict__ states, int64_t D,
         }
         if (!done) atomicExch(err, RQ_E_TABLE);
     }
+}
+
+__global__ void k_fill_u32(uint32_t *p, int64_t n, uint32_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
 }
 
 __global__ void k_filter_build(const uint64_t *__restrict__ s, int64_t D, uint64_t fa, uint64_t fb,
@@ -70,16 +90,18 @@ __global__ void k_filter_build(const uint64_t *__restrict__ s, int64_t D, uint64
 
 constexpr int kSample = 2048;  // shared-memory sample size of the binary-search lookup
 
-template <int LK>
+template <int LK, int KB>
 __global__ void __launch_bounds__(kThreads)
 k_xsource(const rq_subspace_t S, const uint64_t *__restrict__ xm, int J, int32_t *__restrict__ out,
           int *err) {
     __shared__ uint32_t fb[RQ_FILTER_WORDS];
     __shared__ uint64_t samp[LK == RQ_LOOKUP_BSEARCH ? kSample : 1];
+    __shared__ uint32_t T[LK == RQ_LOOKUP_HASH ? kHashTableWords : 1];
     for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) fb[w] = S.fbits[w];
     const int ns = (int)(S.D < kSample ? S.D : kSample);
     if (LK == RQ_LOOKUP_BSEARCH)
         for (int k = threadIdx.x; k < ns; k += blockDim.x) samp[k] = S.states[((int64_t)k * S.D) / ns];
+    if (LK == RQ_LOOKUP_HASH) init_hash_tables(T, KeyWidth<KB>::kNbytes);
     __syncthreads();
     const int64_t total = (int64_t)J * S.D;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
@@ -89,8 +111,13 @@ k_xsource(const rq_subspace_t S, const uint64_t *__restrict__ xm, int J, int32_t
         const uint64_t t = __ldg(S.states + i) ^ __ldg(xm + j);
         int m = -1;
         if (sector_ok(fb, S.fmask_a, S.fmask_b, t)) {
-            if (LK == RQ_LOOKUP_HASH) m = lookup_hash(S, t, err);
-            else m = lookup_bsearch(S, samp, ns, t);
+            if (LK == RQ_LOOKUP_HASH) {
+                if (KB == 64 || (t >> 32) == 0)
+                    m = lookup_hash_at<KB>(S, t, bucket_from_hash(lin_hash(T, t, KeyWidth<KB>::kNbytes),
+                                                                  S.hbits), err);
+            } else {
+                m = lookup_bsearch(S, samp, ns, t);
+            }
         }
         out[idx] = m;
     }
@@ -148,10 +175,12 @@ int grid_for(int64_t n, int per_sm = 8) {
 
 using namespace rq;
 
-RQ_API int rq_subspace_sizes(int64_t D, int32_t *hbits) {
+RQ_API int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits) {
     if (!hbits || D < 1) return fail(RQ_E_ARG, "rq_subspace_sizes: D must be >= 1");
+    if (key_bits != 32 && key_bits != 64) return fail(RQ_E_ARG, "rq_subspace_sizes: key_bits must be 32 or 64");
     int b = 1;
-    while ((int64_t(1) << b) * 2 < D) ++b;  // buckets * 4 slots >= 2 D
+    while ((int64_t(1) << b) * kBucketSlots < 8 * D) ++b;  // load factor <= 1/8
+    if (b > 31) return fail(RQ_E_RANGE, "rq_subspace_sizes: D too large");
     *hbits = b;
     return RQ_OK;
 }
@@ -164,10 +193,13 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     if (sub->lookup != RQ_LOOKUP_HASH && sub->lookup != RQ_LOOKUP_BSEARCH)
         return fail(RQ_E_ARG, "rq_subspace_build: lookup must be RQ_LOOKUP_HASH or RQ_LOOKUP_BSEARCH");
     if (!sub->fbits) return fail(RQ_E_ARG, "rq_subspace_build: fbits is null");
+    if (sub->key_bits != 32 && sub->key_bits != 64)
+        return fail(RQ_E_ARG, "rq_subspace_build: key_bits must be 32 or 64");
+    const int slots = kBucketSlots;
     if (sub->lookup == RQ_LOOKUP_HASH) {
-        if (!sub->hkeys || !sub->hvals || sub->hbits < 1 || sub->hbits > 40)
+        if (!sub->hkeys || !sub->hvals || sub->hbits < 1 || sub->hbits > 31)
             return fail(RQ_E_ARG, "rq_subspace_build: hash buffers missing or hbits out of range");
-        if ((int64_t(4) << sub->hbits) < D + 1)
+        if ((int64_t(slots) << sub->hbits) < D + 1)
             return fail(RQ_E_ARG, "rq_subspace_build: hash table too small for D");
     }
     cudaStream_t st = as_stream(stream);
@@ -186,9 +218,12 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     RQ_CUDA(cudaMemcpyAsync(&last, sub->states + (D - 1), 8, cudaMemcpyDeviceToHost, st));
     RQ_CUDA(cudaStreamSynchronize(st));
     if (h_flag) return fail(RQ_E_UNSORTED, "rq_subspace_build: states are not strictly increasing");
+    const uint64_t top = sub->key_bits == 32 ? 0xFFFFFFFFULL : ~0ULL;
+    if (sub->key_bits == 32 && last > top)
+        return fail(RQ_E_RANGE, "rq_subspace_build: key_bits = 32 needs every state < 2^32");
     uint64_t empty;
-    if (last != ~0ULL) {
-        empty = ~0ULL;
+    if (last != top) {
+        empty = top;
     } else if (first != 0ULL) {
         empty = 0ULL;
     } else {  // both extremes present: the first gap exists because D < 2^64
@@ -199,11 +234,18 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     sub->empty_key = empty;
     RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     if (sub->lookup == RQ_LOOKUP_HASH) {
-        const int64_t slots = int64_t(4) << sub->hbits;
-        k_fill_u64<<<grid_for(slots), kThreads, 0, st>>>(sub->hkeys, slots, empty);
-        k_hash_insert<<<grid_for(D), kThreads, 0, st>>>(
-            sub->states, D, reinterpret_cast<unsigned long long *>(sub->hkeys), sub->hvals,
-            sub->hbits, empty, flag);
+        const int64_t nslots = int64_t(slots) << sub->hbits;
+        if (sub->key_bits == 64) {
+            k_fill_u64<<<grid_for(nslots), kThreads, 0, st>>>(static_cast<uint64_t *>(sub->hkeys),
+                                                              nslots, empty);
+            k_hash_insert<64><<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->hkeys,
+                                                                sub->hvals, sub->hbits, empty, flag);
+        } else {
+            k_fill_u32<<<grid_for(nslots), kThreads, 0, st>>>(static_cast<uint32_t *>(sub->hkeys),
+                                                              nslots, (uint32_t)empty);
+            k_hash_insert<32><<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->hkeys,
+                                                                sub->hvals, sub->hbits, empty, flag);
+        }
         RQ_CUDA(cudaGetLastError());
     }
     RQ_CUDA(cudaMemsetAsync(sub->fbits, 0, RQ_FILTER_WORDS * sizeof(uint32_t), st));
@@ -225,10 +267,12 @@ RQ_API int rq_xsource(const rq_subspace_t *sub, const uint64_t *xmask, int32_t J
     const int g = grid_for(total);
     // the error flag of a hash chain that never ends is dropped here (the table was validated
     // at build time); a null pointer tells the lookup not to report
-    if (sub->lookup == RQ_LOOKUP_HASH)
-        k_xsource<RQ_LOOKUP_HASH><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
+    if (sub->lookup == RQ_LOOKUP_HASH && sub->key_bits == 64)
+        k_xsource<RQ_LOOKUP_HASH, 64><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
+    else if (sub->lookup == RQ_LOOKUP_HASH)
+        k_xsource<RQ_LOOKUP_HASH, 32><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
     else if (sub->lookup == RQ_LOOKUP_BSEARCH)
-        k_xsource<RQ_LOOKUP_BSEARCH><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
+        k_xsource<RQ_LOOKUP_BSEARCH, 64><<<g, kThreads, 0, st>>>(*sub, xmask, J, out, nullptr);
     else
         return fail(RQ_E_ARG, "rq_xsource: unsupported lookup");
     RQ_CUDA(cudaGetLastError());

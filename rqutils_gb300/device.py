@@ -62,7 +62,7 @@ class DeviceSubspace:
     """Sorted distinct states (uint64, bit q = qubit q) with their lookup structures."""
 
     def __init__(self, states, num_qubits=64, lookup='hash', filter_masks=None, device=None,
-                 stream=None):
+                 stream=None, key_bits=None):
         self.device = device or default_device()
         if isinstance(states, torch.Tensor):
             self.states = states.to(self.device, dtype=torch.int64).contiguous()
@@ -73,11 +73,19 @@ class DeviceSubspace:
             raise ValueError('empty subspace')
         self.num_qubits = num_qubits
         self.lookup = {'hash': L.LOOKUP_HASH, 'bsearch': L.LOOKUP_BSEARCH}[lookup]
+        # 32-bit keys when every state and X mask fits (num_qubits <= 32): 8 keys per bucket
+        if key_bits is None:
+            key_bits = 32 if num_qubits <= 32 else 64
+        if key_bits == 32 and num_qubits > 32:
+            raise ValueError('32-bit keys need num_qubits <= 32')
+        self.key_bits = key_bits
         hb = ctypes.c_int32()
-        L.check(L.lib().rq_subspace_sizes(self.D, ctypes.byref(hb)), 'rq_subspace_sizes')
+        L.check(L.lib().rq_subspace_sizes(self.D, key_bits, ctypes.byref(hb)), 'rq_subspace_sizes')
         self.hbits = hb.value
         if self.lookup == L.LOOKUP_HASH:
-            self.hkeys = torch.empty(4 << self.hbits, dtype=torch.int64, device=self.device)
+            # 2^hbits buckets of 4 keys (16 or 32 bytes)
+            self.hkeys = torch.empty((4 * key_bits // 64) << self.hbits, dtype=torch.int64,
+                                     device=self.device)
             self.hvals = torch.empty(4 << self.hbits, dtype=torch.int32, device=self.device)
         else:
             self.hkeys = self.hvals = None
@@ -86,7 +94,7 @@ class DeviceSubspace:
         self.scratch = scratch_tensor(self.D, self.device)
         self.c = L.Subspace(states=L.ptr(self.states), D=self.D, hkeys=L.ptr(self.hkeys),
                             hvals=L.ptr(self.hvals), hbits=self.hbits, lookup=self.lookup,
-                            empty_key=0, fmask_a=int(fa), fmask_b=int(fb), fbits=L.ptr(self.fbits))
+                            key_bits=key_bits, empty_key=0, fmask_a=int(fa), fmask_b=int(fb), fbits=L.ptr(self.fbits))
         L.check(L.lib().rq_subspace_build(ctypes.byref(self.c), L.ptr(self.scratch),
                                           L.stream_ptr(stream)), 'rq_subspace_build')
 

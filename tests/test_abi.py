@@ -49,21 +49,23 @@ def test_host_only_entry_points(libpath):
     from rqutils_gb300 import _lib as L
     lib = L.lib()
     hb = ctypes.c_int32()
-    assert lib.rq_subspace_sizes(1 << 20, ctypes.byref(hb)) == 0
-    assert (4 << hb.value) >= 2 * (1 << 20)
+    assert lib.rq_subspace_sizes(1 << 20, 64, ctypes.byref(hb)) == 0
+    assert (4 << hb.value) >= 8 * (1 << 20) and (4 << (hb.value - 1)) < 8 * (1 << 20)
+    assert lib.rq_subspace_sizes(1 << 20, 32, ctypes.byref(hb)) == 0
+    assert (4 << hb.value) >= 8 * (1 << 20)
     n = ctypes.c_size_t()
     assert lib.rq_scratch_size(1 << 20, ctypes.byref(n)) == 0 and n.value > 0
     prm = L.LobpcgParams(maxiter=10, variant=0, vtype=L.C128, mixed=1)
     assert lib.rq_lobpcg_workspace_size(1000, ctypes.byref(prm), ctypes.byref(n)) == 0
     assert n.value >= 8 * 1000 * 24
-    assert lib.rq_subspace_sizes(0, ctypes.byref(hb)) == L.E_ARG
+    assert lib.rq_subspace_sizes(0, 64, ctypes.byref(hb)) == L.E_ARG
     assert b'D must be' in lib.rq_last_error()
 
 
 def test_struct_layouts():
     from rqutils_gb300 import _lib as L
-    assert ctypes.sizeof(L.Subspace) == 72
+    assert ctypes.sizeof(L.Subspace) == 80
     assert ctypes.sizeof(L.Terms) == 48
-    assert ctypes.sizeof(L.Operator) == 72 + 48 + 8 + 40 + 8
+    assert ctypes.sizeof(L.Operator) == 80 + 48 + 8 + 40 + 8
     assert ctypes.sizeof(L.LobpcgParams) == 64
     assert ctypes.sizeof(L.LobpcgResult) == 48
