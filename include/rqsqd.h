@@ -188,6 +188,18 @@ int rq_lobpcg_workspace_size(int64_t D, const rq_lobpcg_params_t *prm, size_t *b
 int rq_lobpcg_solve(const rq_operator_t *op, const rq_lobpcg_params_t *prm, void *workspace,
                     const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
 
+/* rq_lobpcg_solve without a caller workspace: no counterpart in the reference.  For callers
+ * that cannot allocate device memory (a framework-owned allocator such as an XLA custom-call
+ * handler, work recorded into a CUDA graph, pre-reserved memory).  The workspace is a static
+ * 8 MiB device array of the library, held on every GPU that loads it until the process exits;
+ * problems whose rq_lobpcg_workspace_size exceeds 8 MiB are rejected with RQ_E_RANGE (about
+ * 60,000 rows in complex128, 40,000 with mixed precision).  Runs without CUDA graphs and
+ * allocates nothing.  The first call on a device looks up the array's device address (once per
+ * device); make that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other threads) race and must not be issued. */
+int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_params_t *prm,
+                            const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
+
 /* Matvec supplied by the caller: y = A x in value type vtype on `stream`; return 0 on success. */
 typedef int (*rq_matvec_fn)(void *ctx, int32_t vtype, const void *x, void *y, void *stream);
 

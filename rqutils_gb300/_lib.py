@@ -81,6 +81,8 @@ SIGNATURES = {
     'rq_lobpcg_solve_cb': (ctypes.c_int, [ctypes.c_int64, _c_void_p, _c_void_p, _P(LobpcgParams),
                                           _c_void_p, _c_void_p, _c_void_p, _P(LobpcgResult),
                                           _c_void_p]),
+    'rq_lobpcg_solve_noalloc': (ctypes.c_int, [_P(Operator), _P(LobpcgParams), _c_void_p,
+                                               _c_void_p, _P(LobpcgResult), _c_void_p]),
     'rq_eigenpair_3x3': (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p]),
     'rq_last_error': (ctypes.c_char_p, []),
     'rq_version': (ctypes.c_int, []),

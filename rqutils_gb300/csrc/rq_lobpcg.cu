@@ -16,6 +16,8 @@
 // Mixed precision runs a 32-bit phase first and continues in the 64-bit type from its x and y.
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "rq_common.cuh"
@@ -966,4 +968,68 @@ RQ_API int rq_eigenpair_3x3(const double *mat, double *out, void *stream) {
     k_eig3_abi<<<1, 1, 0, as_stream(stream)>>>(mat, out);
     RQ_CUDA(cudaGetLastError());
     return RQ_OK;
+}
+
+namespace rq {
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free solve
+// ------------------------------------------------------------------------------------------
+// For callers that must not allocate device memory themselves -- code running inside a
+// framework that owns the allocator (an XLA custom-call handler gets only its operand and
+// result buffers), code recorded into a CUDA graph (no allocation while a stream is being
+// captured) or a process whose memory is reserved up front.  The solver's workspace (reduction
+// partials and counters, the matvec's error record, the iteration vectors) lives in this
+// file-scope device array instead of caller memory.  Every GPU that loads the library holds it
+// until the process exits.
+namespace {
+
+constexpr size_t kNoallocBytes = size_t(8) << 20;  // 8 MiB
+static __device__ __align__(256) unsigned char g_noalloc_ws[kNoallocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_ws on the current device.  In host code the symbol is only a
+// host-side stand-in, so the address is looked up once per device (with that device current)
+// and cached.
+int noalloc_workspace(void **out) {
+    int dev = 0;
+    RQ_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(RQ_E_RANGE, "rq_lobpcg_solve_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        RQ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_ws));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return RQ_OK;
+}
+
+}  // namespace
+}  // namespace rq
+
+RQ_API int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_params_t *prm,
+                                   const void *x0, void *x_out, rq_lobpcg_result_t *res,
+                                   void *stream) {
+    if (!op || !prm || !x0 || !x_out || !res)
+        return fail(RQ_E_ARG, "rq_lobpcg_solve_noalloc: null argument");
+    if (op->sub.D < 1) return fail(RQ_E_ARG, "rq_lobpcg_solve_noalloc: D must be >= 1");
+    if (vtype_size(prm->vtype) == 0) return fail(RQ_E_ARG, "rq_lobpcg_solve_noalloc: bad vtype");
+    const size_t need = layout(op->sub.D, *prm).total;
+    if (need > kNoallocBytes)
+        return fail(RQ_E_RANGE,
+                    "rq_lobpcg_solve_noalloc: D = " + std::to_string(op->sub.D) + " needs " +
+                        std::to_string(need) + " bytes of workspace; the static workspace holds " +
+                        std::to_string(kNoallocBytes) + " bytes (use rq_lobpcg_solve)");
+    void *ws = nullptr;
+    RQ_TRY(noalloc_workspace(&ws));
+    // No graph: instantiating one may allocate device memory.  The workspace carries the last
+    // call's contents; solve() clears the reduction counter and the error record it relies on.
+    rq_lobpcg_params_t p = *prm;
+    p.use_graph = 0;
+    return solve_entry(op, nullptr, nullptr, &p, ws, x0, x_out, res, stream);
 }
