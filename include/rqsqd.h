@@ -165,7 +165,9 @@ typedef struct rq_lobpcg_params {
     int32_t refresh;        /* FAST: recompute A x, A y every `refresh` iterations (0 = 32)  */
     int32_t use_graph;      /* 1: run the loop as one CUDA graph with a device-side while    */
     int32_t jacobi;         /* 1: precondition the residual with (diag(H) - theta)^-1        */
-    int32_t pad_;
+    int32_t guard;          /* 1: where the reference arithmetic gives 0/0 (a degenerate
+                               Cardano eigenvector, |s| = 0) take a finite replacement; only
+                               results that would otherwise be NaN change                    */
 } rq_lobpcg_params_t;
 
 typedef struct rq_lobpcg_result {

@@ -56,7 +56,8 @@ struct State {
     int since_refresh, want_refresh;
     int variant, matvecs;
     int certify;  // FAST: the last convergence candidate must be confirmed by fresh products
-    int pad_[3];
+    int guard;    // replace 0/0 breakdowns (degenerate Cardano eigenvector, |s| = 0)
+    int pad_[2];
 };
 
 // ------------------------------------------------------------------------------------------
@@ -282,6 +283,7 @@ k_upd_tu(State *st, int64_t D, const V *x, const V *y, const V *p, void *red) {
     GATE(st);
     using R = typename VT<V>::R;
     const double ns = sqrt(st->red[kSn].x);
+    const bool keep_y = st->guard && ns == 0.;  // s = 0: y' = y instead of 0 * inf
     const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
     const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
     const cx<R> mns = {(R)(-ns), (R)0};
@@ -289,7 +291,7 @@ k_upd_tu(State *st, int64_t D, const V *x, const V *y, const V *p, void *red) {
     GRID_LOOP(i, D) {
         const cx<R> xi = VT<V>::ld(x, i);
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
-        const cx<R> t = axpy(mns, xi, cmul(k0s, s));
+        const cx<R> t = keep_y ? VT<V>::ld(y, i) : axpy(mns, xi, cmul(k0s, s));
         const cx<R> u = axpy(k0, xi, s);
         tn.add(t, t, VT<V>::kComplex);
         un.add(u, u, VT<V>::kComplex);
@@ -305,6 +307,7 @@ k_upd_xy(State *st, int64_t D, V *x, V *y, const V *p, V *ax, V *ay, const V *ap
     GATE(st);
     using R = typename VT<V>::R;
     const double ns = sqrt(st->red[kSn].x);
+    const bool keep_y = st->guard && ns == 0.;  // s = 0: y' = y instead of 0 * inf
     const double it = 1. / sqrt(st->red[kTn].x), iu = 1. / sqrt(st->red[kUn].x);
     const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
     const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
@@ -312,15 +315,17 @@ k_upd_xy(State *st, int64_t D, V *x, V *y, const V *p, V *ax, V *ay, const V *ap
     const R rit = (R)it, riu = (R)iu;
     GRID_LOOP(i, D) {
         const cx<R> xi = VT<V>::ld(x, i);
-        const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
-        const cx<R> t = axpy(mns, xi, cmul(k0s, s));
+        const cx<R> yi = VT<V>::ld(y, i);
+        const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, yi));
+        const cx<R> t = keep_y ? yi : axpy(mns, xi, cmul(k0s, s));
         const cx<R> u = axpy(k0, xi, s);
         VT<V>::st(x, i, {u.re * riu, u.im * riu});
         VT<V>::st(y, i, {t.re * rit, t.im * rit});
         if (CARRY) {
             const cx<R> axi = VT<V>::ld(ax, i);
-            const cx<R> as = axpy(k2, VT<V>::ld(ap, i), cmul(k1, VT<V>::ld(ay, i)));
-            const cx<R> at = axpy(mns, axi, cmul(k0s, as));
+            const cx<R> ayi = VT<V>::ld(ay, i);
+            const cx<R> as = axpy(k2, VT<V>::ld(ap, i), cmul(k1, ayi));
+            const cx<R> at = keep_y ? ayi : axpy(mns, axi, cmul(k0s, as));
             const cx<R> au = axpy(k0, axi, as);
             VT<V>::st(ax, i, {au.re * riu, au.im * riu});
             VT<V>::st(ay, i, {at.re * rit, at.im * rit});
@@ -426,7 +431,7 @@ __global__ void __launch_bounds__(kThreads) k_copy(State *st, int64_t D, const V
 // Lowest eigenpair of a Hermitian 3x3 given by its strict lower triangle (m10, m20, m21) and its
 // diagonal (complex values, real part used as in ground_locg.py:446); Cardano (Kopp 2008).
 __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2 m11, double2 m22,
-                     double &lam, double2 (&v)[3]) {
+                     double &lam, double2 (&v)[3], bool guard = false) {
     const double d0 = m00.x, d1 = m11.x, d2 = m22.x;
     const double a10 = m10.x * m10.x + m10.y * m10.y;
     const double a20 = m20.x * m20.x + m20.y * m20.y;
@@ -463,6 +468,35 @@ __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2
         nrm += c[k].x * c[k].x + c[k].y * c[k].y;
     }
     nrm = sqrt(nrm);
+    if (guard && !(nrm > 0. && isfinite(nrm)) && isfinite(lam)) {
+        // columns 1 and 2 of (A - lambda I) are parallel (or zero): the eigenvector is
+        // orthogonal to the other column pairs; take the larger of their cross products
+        const double2 z0 = make_double2(m00.x - lam, m00.y);
+        const double2 col0[3] = {z0, m10, m20};
+        const double2 col1[3] = {a0, a1, a2};
+        const double2 col2[3] = {b0, b1, b2};
+        double best = 0.;
+        for (int pair = 0; pair < 2; ++pair) {
+            const double2 *u = col0, *w = pair == 0 ? col1 : col2;
+            double2 e[3] = {sub(mul(u[1], w[2]), mul(u[2], w[1])), sub(mul(u[2], w[0]), mul(u[0], w[2])),
+                            sub(mul(u[0], w[1]), mul(u[1], w[0]))};
+            double n2 = 0.;
+            for (int k = 0; k < 3; ++k) {
+                e[k].y = -e[k].y;
+                n2 += e[k].x * e[k].x + e[k].y * e[k].y;
+            }
+            if (n2 > best && isfinite(n2)) {
+                best = n2;
+                for (int k = 0; k < 3; ++k) c[k] = e[k];
+            }
+        }
+        nrm = sqrt(best);
+        if (!(nrm > 0.)) {  // A = lambda I on the span: any vector; keep x
+            c[0] = make_double2(1., 0.);
+            c[1] = c[2] = make_double2(0., 0.);
+            nrm = 1.;
+        }
+    }
     for (int k = 0; k < 3; ++k) v[k] = make_double2(c[k].x / nrm, c[k].y / nrm);
 }
 
@@ -471,7 +505,7 @@ __global__ void k_rr3(State *st) {
     double lam;
     double2 v[3];
     eig3(st->red[kG10], st->red[kG20], st->red[kG21], st->red[kG00], st->red[kG11], st->red[kG22],
-         lam, v);
+         lam, v, st->guard != 0);
     st->theta = lam;
     for (int k = 0; k < 3; ++k) st->kappa[k] = v[k];
 }
@@ -685,8 +719,9 @@ struct Phase {
         return RQ_OK;
     }
 
-    // iterations 0 and 1 from v.x (unnormalised), ground_locg.py:264-286, 346
-    int start(cudaStream_t s) {
+    // iterations 0 and 1 from v.x (unnormalised), ground_locg.py:264-286, 346; FAST also needs
+    // A y for its carried products
+    int start(int variant, cudaStream_t s) {
         Pairs<V, 1> nx{{v.x}, {v.x}};
         k_dots<V, 1><<<grid, kThreads, 0, s>>>(st, D, nx, kMisc2, red);
         k_normalize<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.x, kMisc2);
@@ -703,6 +738,7 @@ struct Phase {
         k_upd2_norms<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.p, red);
         k_upd2_xy<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p);
         RQ_TRY(matvec(v.x, v.ax, s));
+        if (variant == RQ_LOBPCG_FAST) RQ_TRY(matvec(v.y, v.ay, s));
         k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
         RQ_CUDA(cudaGetLastError());
         return RQ_OK;
@@ -800,6 +836,7 @@ int init_state(State *st, const rq_lobpcg_params_t &p, double tol, double tol_di
     h.phase_lo = lo ? 1 : 0;
     h.refresh = p.refresh > 0 ? p.refresh : 32;
     h.variant = p.variant;
+    h.guard = p.guard;
     RQ_CUDA(cudaMemcpyAsync(st, &h, sizeof(State), cudaMemcpyHostToDevice, s));
     RQ_CUDA(cudaStreamSynchronize(s));  // h is a stack object
     return RQ_OK;
@@ -834,7 +871,7 @@ int solve(const rq_operator_t &op, rq_matvec_fn fn, void *ctx, const rq_lobpcg_p
                       carve_vecs<VLO>(ws + L.vec_lo, L.lo_bytes), D, grid, jac, op.diag0};
         RQ_TRY(init_state<VLO>(st, p, 1.1920928955078125e-07, tol_dim, true, p.maxiter, s));
         k_convert<VHI, VLO><<<grid, kThreads, 0, s>>>(D, static_cast<const VHI *>(x0), lo.v.x);
-        RQ_TRY(lo.start(s));
+        RQ_TRY(lo.start(p.variant, s));
         if (p.maxiter > 0) RQ_TRY(run_loop<VLO>(lo, p.variant, p.use_graph != 0, s));
         HostState h{};
         RQ_TRY(read_flags(st, h, s));
@@ -852,7 +889,7 @@ int solve(const rq_operator_t &op, rq_matvec_fn fn, void *ctx, const rq_lobpcg_p
     } else {
         RQ_TRY(init_state<VHI>(st, p, tol, tol_dim, false, p.maxiter, s));
         RQ_CUDA(cudaMemcpyAsync(hi.v.x, x0, L.hi_bytes, cudaMemcpyDeviceToDevice, s));
-        RQ_TRY(hi.start(s));
+        RQ_TRY(hi.start(p.variant, s));
     }
     if (p.maxiter > 0) RQ_TRY(run_loop<VHI>(hi, p.variant, p.use_graph != 0, s));
     State h{};

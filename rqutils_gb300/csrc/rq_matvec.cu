@@ -212,61 +212,63 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
                 if (!d0 && skip >= g0 && skip < g1)
                     add_group<R>(tl.cf, tl.zm, tl.off[skip - g0], tl.off[skip - g0 + 1], s64,
                                  VT<V>::ld(x, i), true, acc);
-                int g = g0;
-                for (; g + U <= g1; g += U) {
-                    K t[U];
-                    uint32_t b[U];
-                    bool q[U];
-                    typename KeyWidth<KB>::Bucket w[U];
+                // Probe in super-chunks of 64 groups.  The probe loop only marks "hot" groups
+                // (a key match, a full bucket, or a target equal to the empty key) in a 64-bit
+                // mask; the hot groups are resolved afterwards, so the rare divergent work runs
+                // once per super-chunk instead of inside every probe step.
+                for (int gs0 = g0; gs0 < g1; gs0 += 64) {
+                    const int gs1 = min(g1, gs0 + 64);
+                    uint64_t hot = 0ULL;
+                    int g = gs0;
+                    for (; g + U <= gs1; g += U) {
+                        K t[U];
+                        uint32_t b[U];
+                        bool q[U];
+                        typename KeyWidth<KB>::Bucket w[U];
 #pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        const int gl = g + u - g0;
-                        uint32_t hxg;
-                        if (KB == 32) {
-                            const uint2 e = tl.gs[gl];
-                            t[u] = s ^ (K)e.x;
-                            hxg = e.y;
-                        } else {
-                            t[u] = s ^ (K)tl.xm[gl];
-                            hxg = tl.hx[gl];
+                        for (int u = 0; u < U; ++u) {
+                            const int gl = g + u - g0;
+                            uint32_t hxg;
+                            if (KB == 32) {
+                                const uint2 e = tl.gs[gl];
+                                t[u] = s ^ (K)e.x;
+                                hxg = e.y;
+                            } else {
+                                t[u] = s ^ (K)tl.xm[gl];
+                                hxg = tl.hx[gl];
+                            }
+                            q[u] = (g + u != skip);
+                            if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
+                            b[u] = (hs ^ hxg) >> shift;
                         }
-                        q[u] = (g + u != skip);
-                        if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
-                        b[u] = (hs ^ hxg) >> shift;
-                    }
 #pragma unroll
-                    for (int u = 0; u < U; ++u)
-                        w[u] = KeyWidth<KB>::load(keys + (size_t)b[u] * kBucketBytes, q[u],
-                                                  S.empty_key);
+                        for (int u = 0; u < U; ++u)
+                            w[u] = KeyWidth<KB>::load(keys + (size_t)b[u] * kBucketBytes, q[u],
+                                                      S.empty_key);
 #pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        bool any, open;
-                        test_bucket(w[u], t[u], empty, any, open);
-                        // rare: a hit, a full bucket, or a target equal to the empty key
-                        if (q[u] && (any || !open)) {
-                            int m = -1;
-                            if (t[u] != empty) {
-                                const int sl = slot_of(w[u], t[u]);
-                                if (sl >= 0) m = __ldg(S.hvals + (size_t)b[u] * kBucketSlots + sl);
-                                else if (!open) m = probe_rest<KB>(S, (uint64_t)t[u], b[u], err);
-                            }
-                            if (m >= 0) {
-                                const int gl = g + u - g0;
-                                add_group<R>(tl.cf, tl.zm, tl.off[gl], tl.off[gl + 1], s64,
-                                             VT<V>::ld(x, m), true, acc);
-                            }
+                        for (int u = 0; u < U; ++u) {
+                            bool any, open;
+                            test_bucket(w[u], t[u], empty, any, open);
+                            hot |= (uint64_t)(q[u] && (any || !open)) << (g + u - gs0);
                         }
                     }
-                }
-                for (; g < g1; ++g) {
-                    if (g == skip) continue;
-                    const int gl = g - g0;
-                    const K t = s ^ (K)tl.xm[gl];
-                    if (t == empty || (FILTER && !sector_ok_k<K>(fb, fa, fbm, t))) continue;
-                    const int m = lookup_hash_at<KB>(S, (uint64_t)t, (hs ^ tl.hx[gl]) >> shift, err);
-                    if (m >= 0)
-                        add_group<R>(tl.cf, tl.zm, tl.off[gl], tl.off[gl + 1], s64, VT<V>::ld(x, m),
-                                     true, acc);
+                    for (; g < gs1; ++g) {  // tail of the super-chunk
+                        const int gl = g - g0;
+                        const K t = s ^ (K)tl.xm[gl];
+                        bool ok = (g != skip);
+                        if (FILTER) ok = ok && sector_ok_k<K>(fb, fa, fbm, t);
+                        if (ok) hot |= 1ULL << (g - gs0);
+                    }
+                    while (hot) {
+                        const int bit = __ffsll((long long)hot) - 1;
+                        hot &= hot - 1ULL;
+                        const int gl = gs0 + bit - g0;
+                        const K t = s ^ (K)tl.xm[gl];
+                        const int m = lookup_hash_at<KB>(S, (uint64_t)t, (hs ^ tl.hx[gl]) >> shift, err);
+                        if (m >= 0)
+                            add_group<R>(tl.cf, tl.zm, tl.off[gl], tl.off[gl + 1], s64,
+                                         VT<V>::ld(x, m), true, acc);
+                    }
                 }
             }
             if (g1 >= T.J) break;

@@ -9,14 +9,25 @@ namespace rq {
 
 namespace {
 
-__global__ void k_check_sorted(const uint64_t *__restrict__ s, int64_t D, int *flag,
-                               unsigned long long *gap) {
+__global__ void k_check_sorted(const uint64_t *__restrict__ s, int64_t D, int *flag) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i + 1 < D;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t a = s[i], b = s[i + 1];
-        if (a >= b) atomicExch(flag, 1);
-        if (b != a + 1) atomicMin(gap, (unsigned long long)i);
-    }
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (s[i] >= s[i + 1]) atomicExch(flag, 1);
+}
+
+// First index i with s[i + 1] != s[i] + 1 (only needed when both 0 and the top key are states).
+// One atomic per block after a block-wide minimum.
+__global__ void k_first_gap(const uint64_t *__restrict__ s, int64_t D, unsigned long long *gap) {
+    __shared__ unsigned long long best;
+    if (threadIdx.x == 0) best = ~0ULL;
+    __syncthreads();
+    unsigned long long mine = ~0ULL;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i + 1 < D;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (s[i + 1] != s[i] + 1 && (unsigned long long)i < mine) mine = (unsigned long long)i;
+    if (mine != ~0ULL) atomicMin(&best, mine);
+    __syncthreads();
+    if (threadIdx.x == 0 && best != ~0ULL) atomicMin(gap, best);
 }
 
 __global__ void k_fill_u64(uint64_t *p, int64_t n, uint64_t v) {
@@ -207,7 +218,7 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
     RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     RQ_CUDA(cudaMemsetAsync(gap, 0xff, sizeof(unsigned long long), st));
-    k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, flag, gap);
+    k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, flag);
     RQ_CUDA(cudaGetLastError());
     int h_flag = 0;
     unsigned long long h_gap = 0;
@@ -227,6 +238,9 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     } else if (first != 0ULL) {
         empty = 0ULL;
     } else {  // both extremes present: the first gap exists because D < 2^64
+        k_first_gap<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, gap);
+        RQ_CUDA(cudaMemcpyAsync(&h_gap, gap, sizeof(h_gap), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaStreamSynchronize(st));
         uint64_t below = 0;
         RQ_CUDA(cudaMemcpy(&below, sub->states + h_gap, 8, cudaMemcpyDeviceToHost));
         empty = below + 1;

@@ -31,12 +31,13 @@ _VARIANTS = {'reference': L.LOBPCG_REFERENCE, 'fast': L.LOBPCG_FAST}
 
 
 def _params(D, vtype, maxiter, tol, tol_dim, variant, mixed, target_rel, switch_rel, refresh,
-            use_graph, jacobi):
+            use_graph, jacobi, guard=True):
     return L.LobpcgParams(maxiter=int(maxiter), variant=_VARIANTS[variant], vtype=vtype,
                           mixed=int(bool(mixed)), tol=float(tol or 0.),
                           tol_dim=float(tol_dim or 0.), switch_rel=float(switch_rel),
                           target_rel=float(target_rel or 0.), refresh=int(refresh),
-                          use_graph=int(bool(use_graph)), jacobi=int(bool(jacobi)))
+                          use_graph=int(bool(use_graph)), jacobi=int(bool(jacobi)),
+                          guard=int(bool(guard)))
 
 
 def _workspace(owner, D, prm, device):
@@ -58,13 +59,13 @@ def _info(res):
 
 def lobpcg_solve(op: DeviceOperator, x0, maxiter=1000, tol=None, tol_dim=None,
                  variant='reference', mixed=False, target_rel=None, switch_rel=1e-5, refresh=32,
-                 use_graph=True, jacobi=False, stream=None):
+                 use_graph=True, jacobi=False, guard=True, stream=None):
     """Run rq_lobpcg_solve on a DeviceOperator from the device vector x0 (its dtype selects the
     value type).  Returns (eigval, x, info)."""
     x0 = x0.contiguous()
     vt = VTYPE_OF[x0.dtype]
     prm = _params(op.D, vt, maxiter, tol, tol_dim, variant, mixed, target_rel, switch_rel,
-                  refresh, use_graph, jacobi)
+                  refresh, use_graph, jacobi, guard)
     ws = _workspace(op, op.D, prm, op.device)
     xout = torch.empty_like(x0)
     res = L.LobpcgResult()
