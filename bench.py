@@ -1,9 +1,11 @@
 """Benchmark of the SQD hot path on one GB300.
 
-Workload (the configuration the headline metric is quoted on): Fermi-Hubbard 4x4, periodic,
-t = 1, U = 4, Jordan-Wigner mapped to 32 qubits (65 X groups, 177 terms after consolidation);
-subspace of D = 2^20 bitstrings drawn uniformly without replacement from the 8-up / 8-down sector
-(seed 1); complex64 vectors with FP32 compensated accumulation.
+Workload (the configuration the headline metric is quoted on, ``--workload hubbard``):
+Fermi-Hubbard 4x4, periodic, t = 1, U = 4, Jordan-Wigner mapped to 32 qubits (65 X groups, 177
+terms after consolidation); subspace of D = 2^20 bitstrings drawn uniformly without replacement
+from the 8-up / 8-down sector (seed 1); complex64 vectors with FP32 compensated accumulation.
+``--workload chemistry`` (64 qubits, 50,000 terms, D = 2^26) and ``--workload random20``
+(20 qubits, 200 terms, D = 16384, complex128) run the other configurations through the same code.
 
 A step is one matrix-free Pauli-sum matvec y = H x over the whole subspace (hash lookups, the
 reference's cache_level (0, *) path) with x resident in HBM.  Between timed steps a 256 MiB buffer
@@ -32,31 +34,60 @@ sys.path.insert(0, ROOT)
 
 METRIC = 'Pauli-matvec/s & time-to-residual 1e-8 (learned warm-start vs plain), 1 GB300'
 UNIT = 'matvec/s'
-D_BENCH = 1 << 20
-SEED = 1
 L2_FLUSH_BYTES = 256 << 20
 PROFILE_TRAFFIC = os.path.join(ROOT, 'profiles', 'matvec_free_hubbard4x4_D1048576.txt')
 
 
-def workload():
-    from rqutils_gb300 import workloads
-    from rqutils_gb300.paulis.symplectic import PauliSumXZ
-    p, c = workloads.hubbard_jw(4, 4, 1.0, 4.0, periodic=True)
-    ham = PauliSumXZ.from_paulisum((p, c), force_real=True, add_padding=True)
-    rng = np.random.default_rng(SEED)
-    S = workloads.sample_sector(rng, D_BENCH, [(16, 8), (16, 8)])
-    x = workloads.random_vector(np.random.default_rng(SEED + 1), D_BENCH, complex_=True)
-    return ham, S, x
+class Workload:
+    """One benchmark configuration: Hamiltonian, sorted subspace, input vector, value type."""
 
+    def __init__(self, name, rows=None):
+        from rqutils_gb300 import workloads as W
+        from rqutils_gb300.paulis.symplectic import PauliSumXZ
+        self.name = name
+        if name == 'hubbard':
+            # Fermi-Hubbard 4x4 periodic, t=1, U=4, 32 spin-orbitals; D = 2^20 from 8 up / 8 down
+            p, c = W.hubbard_jw(4, 4, 1.0, 4.0, periodic=True)
+            self.D, self.seed = 1 << 20, 1
+            self.blocks = [(16, 8), (16, 8)]
+            self.vtype = 'c64'
+            self.label = 'hubbard4x4_periodic_t1_U4_jw32_D1048576_sector8u8d'
+            self.lobpcg = True
+        elif name == 'chemistry':
+            # 32 spatial orbitals -> 64 spin-orbitals, top 50,000 |c|; D = 2^26 at 16 a + 16 b
+            p, c = W.chemistry_jw(32, np.random.default_rng(4), keep=50000)
+            self.D, self.seed = 1 << 26, 5
+            self.blocks = [(32, 16), (32, 16)]
+            self.vtype = 'c64'
+            self.label = 'chemistry32orb_jw64_K50000_D67108864_sector16a16b'
+            self.lobpcg = False
+        elif name == 'random20':
+            # 20 qubits, K = 200 local terms (locality 1..4, N(0,1)); D = 16384 at weight 10
+            p, c = W.random_pauli_sum(np.random.default_rng(20), 20, 200)
+            self.D, self.seed = 16384, 20
+            self.blocks = [(20, 10)]
+            self.vtype = 'c128'
+            self.label = 'random20_K200_loc1to4_D16384_weight10'
+            self.lobpcg = True
+        else:
+            raise ValueError(f'unknown workload {name}')
+        if rows:  # reduced subspace for profiling captures
+            self.D = int(rows)
+            self.label += f'_rows{self.D}'
+        self.ham = PauliSumXZ.from_paulisum((p, c), force_real=True, add_padding=True)
+        self.nq = self.ham.num_qubits
+        self.S = W.sample_sector(np.random.default_rng(self.seed), self.D, self.blocks)
+        self.x = W.random_vector(np.random.default_rng(self.seed + 1), self.D, complex_=True)
 
-def config(extra=None):
-    cfg = {'workload': 'hubbard4x4_periodic_t1_U4_jw32_D1048576_sector8u8d',
-           'D': D_BENCH, 'num_qubits': 32, 'groups': 65, 'terms': 177,
-           'matvec_mode': 'matrix-free (hash lookup, sector filter)',
-           'l2_policy': 'flush 256 MiB between timed steps', 'seed': SEED}
-    if extra:
-        cfg.update(extra)
-    return cfg
+    def config(self, extra=None):
+        J = len(self.ham.xmask)
+        cfg = {'workload': self.label, 'D': self.D, 'num_qubits': self.nq, 'groups': J,
+               'terms': len(self.ham.zmask), 'vector_type': self.vtype,
+               'matvec_mode': 'matrix-free (hash lookup, sector filter)',
+               'l2_policy': 'flush 256 MiB between timed steps', 'seed': self.seed}
+        if extra:
+            cfg.update(extra)
+        return cfg
 
 
 # ---------------------------------------------------------------------------------------------
@@ -199,15 +230,18 @@ def run_ours(args, rank, ws):
     from rqutils_gb300.ground_locg import lobpcg_solve
 
     dev = torch.device('cuda', torch.cuda.current_device())
-    ham, S, xh = workload()
-    terms = DeviceTerms(ham, device=dev)
-    sub = DeviceSubspace(S, num_qubits=32, device=dev)
+    wl = Workload(args.workload, args.rows)
+    tdt = torch.complex64 if wl.vtype == 'c64' else torch.complex128
+    bv = 8 if wl.vtype == 'c64' else 16
+    terms = DeviceTerms(wl.ham, device=dev)
+    sub = DeviceSubspace(wl.S, num_qubits=wl.nq, device=dev)
     op_free = DeviceOperator(terms, sub, mode='free')
     op_conn = DeviceOperator(terms, sub, mode='conn')
-    op_csr = DeviceOperator(terms, sub, mode='csr', csr_vtype=2)
+    small = wl.D <= (1 << 22)
+    op_csr = DeviceOperator(terms, sub, mode='csr', csr_vtype=2 if bv == 8 else 3) if small else None
     hits = op_conn.nnz
     D, J, J0 = sub.D, terms.J, 1 if terms.diag_group >= 0 else 0
-    x = torch.as_tensor(xh).to(dev, torch.complex64)
+    x = torch.as_tensor(wl.x).to(dev, tdt)
     y = torch.empty_like(x)
     flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
@@ -238,20 +272,28 @@ def run_ours(args, rank, ws):
     rel = float(torch.linalg.vector_norm(y - y_conn) / torch.linalg.vector_norm(y_conn))
 
     # other modes (same flush policy)
-    for op in (op_conn, op_csr):
+    modes = {}
+    nsteps_m = max(3, min(args.steps, 20))
+    for name, op in (('conn', op_conn), ('csr', op_csr)):
+        if op is None:
+            continue
         for _ in range(args.warmup):
             op.matvec(x, out=y)
-    t_conn = statistics.mean(time_steps(lambda: op_conn.matvec(x, out=y), args.steps, flush, stream))
-    t_csr = statistics.mean(time_steps(lambda: op_csr.matvec(x, out=y), args.steps, flush, stream))
-    # matrix-free without the sector filter (every off-diagonal lookup probes the table)
-    sub_nf = DeviceSubspace(S, num_qubits=32, device=dev, filter_masks=(0, 0))
-    op_nf = DeviceOperator(terms, sub_nf, mode='free')
-    for _ in range(args.warmup):
-        op_nf.matvec(x, out=y)
-    t_nf = statistics.mean(time_steps(lambda: op_nf.matvec(x, out=y), args.steps, flush, stream))
+        t = statistics.mean(time_steps(lambda: op.matvec(x, out=y), nsteps_m, flush, stream))
+        modes[f'{name}_matvec_per_s'] = 1e3 / t
+    if small:
+        # matrix-free without the sector filter (every off-diagonal lookup probes the table)
+        sub_nf = DeviceSubspace(wl.S, num_qubits=wl.nq, device=dev, filter_masks=(0, 0))
+        op_nf = DeviceOperator(terms, sub_nf, mode='free')
+        for _ in range(args.warmup):
+            op_nf.matvec(x, out=y)
+        t_nf = statistics.mean(time_steps(lambda: op_nf.matvec(x, out=y), nsteps_m, flush, stream))
+        modes['free_nofilter_matvec_per_s'] = 1e3 / t_nf
+        del op_nf, sub_nf
+    modes['free_vs_conn_rel_diff'] = rel
 
     # e2e through the public API with host buffers
-    xh_pin = torch.as_tensor(xh.astype(np.complex64)).pin_memory()
+    xh_pin = torch.as_tensor(wl.x.astype(np.complex64 if bv == 8 else np.complex128)).pin_memory()
     yh_pin = torch.empty_like(xh_pin).pin_memory()
     xd = torch.empty_like(x)
 
@@ -268,54 +310,61 @@ def run_ours(args, rank, ws):
     e2e_value = ws * args.steps / e2e_t
 
     # roofline of the matvec kernel
-    bv = 8
     abytes = algorithmic_bytes(D, J, J0, hits, bv)
     peak, peak_kind = measured_peaks()
     achieved = abytes / (ms_per_step / 1e3) / 1e9
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic() if wl.name == 'hubbard' else None
 
-    # LOBPCG time to a relative residual of 1e-8 from a seeded random start.  (The reference's
-    # one-hot start at the lowest diagonal entry is an isolated state of this subspace -- an exact
-    # eigenvector with zero residual -- on which its Rayleigh-Ritz step breaks down.)
     lob = {}
-    xr = np.random.default_rng(SEED + 2).normal(size=D)
-    for name, kw in (('mixed_fast', dict(mixed=True, variant='fast')),
-                     ('fp64_fast', dict(mixed=False, variant='fast')),
-                     ('fp64_reference', dict(mixed=False, variant='reference'))):
-        x0 = torch.as_tensor(xr, dtype=torch.float64, device=dev)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        eig, xs, info = lobpcg_solve(op_conn, x0, maxiter=3000, target_rel=1e-8, **kw)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        # certify: FP64 residual with a fresh FP64 matvec
-        ax = op_conn.matvec(xs)
-        r = float(torch.linalg.vector_norm(ax - eig * xs))
-        lob[name] = {'start': 'random (seeded)', 'time_s': round(dt, 4), 'iterations': info['niter'],
-                     'iterations_32bit': info['niter_lo'], 'eigval': eig,
-                     'rel_residual_fp64': r / abs(eig), 'converged': info['converged']}
+    if wl.lobpcg:
+        # LOBPCG time to a relative residual of 1e-8 from a seeded random start.  (The
+        # reference's one-hot start at the lowest diagonal entry can be an isolated state of a
+        # sparse subspace -- an exact eigenvector with zero residual -- on which its
+        # Rayleigh-Ritz step breaks down.)
+        real = terms.is_real
+        ldt = torch.float64 if real else torch.complex128
+        rng = np.random.default_rng(wl.seed + 2)
+        xr = rng.normal(size=D) if real else rng.normal(size=D) + 1j * rng.normal(size=D)
+        variants = [('mixed_fast', dict(mixed=True, variant='fast')),
+                    ('fp64_fast', dict(mixed=False, variant='fast')),
+                    ('fp64_reference', dict(mixed=False, variant='reference'))]
+        if wl.name == 'random20':
+            # Jacobi helps here; on the Hubbard subspace the diagonal (U x double occupancy) is
+            # massively degenerate and (d - theta)^-1 stalls the iteration near a diagonal level
+            variants.append(('fp64_fast_jacobi', dict(mixed=False, variant='fast', jacobi=True)))
+        for name, kw in variants:
+            x0 = torch.as_tensor(xr, dtype=ldt, device=dev)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eig, xs, info = lobpcg_solve(op_conn, x0, maxiter=5000, target_rel=1e-8, **kw)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            ax = op_conn.matvec(xs)  # certify with a fresh FP64 matvec
+            r = float(torch.linalg.vector_norm(ax - eig * xs))
+            lob[name] = {'start': 'random (seeded)', 'time_s': round(dt, 4),
+                         'iterations': info['niter'], 'iterations_32bit': info['niter_lo'],
+                         'eigval': eig, 'rel_residual_fp64': r / abs(eig),
+                         'converged': info['converged']}
 
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True,
-        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic',
-        'config': config({'parallelism': f'replicas{ws}' if ws > 1 else 'single',
-                          'hits_per_matvec': hits, 'wall_s_timed_region': round(wall, 3)}),
-        'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': 8 * D,
-                'd2h_bytes_per_step': 8 * D},
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': wl.vtype, 'data': 'synthetic',
+        'config': wl.config({'parallelism': f'replicas{ws}' if ws > 1 else 'single',
+                             'hits_per_matvec': hits, 'wall_s_timed_region': round(wall, 3)}),
+        'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': bv * D,
+                'd2h_bytes_per_step': bv * D},
         'gpu_launches': args.steps,
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'traffic': traffic,
                      'peak_source': f'{peak_kind} hbm_gbs',
                      'algorithmic_bytes_per_launch': abytes},
-        'modes': {'conn_matvec_per_s': 1e3 / t_conn, 'csr_matvec_per_s': 1e3 / t_csr,
-                  'free_nofilter_matvec_per_s': 1e3 / t_nf,
-                  'free_vs_conn_rel_diff': rel},
+        'modes': modes,
         'lobpcg': lob,
         'clocks': clk.summary(),
     }
     if rank == 0:
-        line['cpu_baseline'] = cpu_baseline(ham, S, xh, steps=6)
+        line['cpu_baseline'] = cpu_baseline(wl, budget_s=12.0)
         print(json.dumps(line), flush=True)
 
 
@@ -325,11 +374,11 @@ def run_profile(args):
     import torch
     from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
     dev = torch.device('cuda', torch.cuda.current_device())
-    ham, S, xh = workload()
-    terms = DeviceTerms(ham, device=dev)
-    sub = DeviceSubspace(S, num_qubits=32, device=dev)
+    wl = Workload(args.workload, args.rows)
+    terms = DeviceTerms(wl.ham, device=dev)
+    sub = DeviceSubspace(wl.S, num_qubits=wl.nq, device=dev)
     op = DeviceOperator(terms, sub, mode='free')
-    x = torch.as_tensor(xh).to(dev, torch.complex64)
+    x = torch.as_tensor(wl.x).to(dev, torch.complex64 if wl.vtype == 'c64' else torch.complex128)
     y = torch.empty_like(x)
     flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
@@ -343,7 +392,7 @@ def run_profile(args):
 # ---------------------------------------------------------------------------------------------
 # CPU baseline / reference arm: the oracle's restatement of the reference matvec
 # ---------------------------------------------------------------------------------------------
-def _oracle_setup(ham, S):
+def _oracle_setup(ham):
     from oracle.paulis import OracleTerms
     J = len(ham.xmask)
     counts = np.diff(ham.toff)
@@ -357,38 +406,72 @@ def _oracle_setup(ham, S):
     return OracleTerms(x=ham.xmask.copy(), z=z, c=c, counts=counts, num_qubits=ham.num_qubits)
 
 
-def cpu_baseline(ham, S, xh, steps=1):
-    """apply_h (sqd.py:590-605, X sources re-derived by sort-merge every matvec) restated in
-    NumPy, on all host cores (groups split over a thread pool), for `steps` full matvecs."""
+def cpu_baseline(wl, budget_s=12.0, steps=None):
+    """apply_h (sqd.py:590-605: X sources re-derived by sort-merge in every matvec) restated in
+    NumPy, complex128, on all host cores (groups split over a thread pool).  Bounded sample:
+    whole matvecs while they fit the time budget, else a prefix of the X groups timed and scaled
+    to all groups (the cost is linear in the number of groups)."""
     from oracle.sqd import matvec_nocache
-    terms = _oracle_setup(ham, S)
+    terms = _oracle_setup(wl.ham)
     cores = os.cpu_count() or 1
-    x = xh.astype(np.complex128)
+    x = wl.x.astype(np.complex128)
+    J = len(terms.x)
+    # probe the cost of one group first (single thread), then of a chunk of groups
+    one = type(terms)(x=terms.x[:1], z=terms.z[:1], c=terms.c[:1], counts=terms.counts[:1],
+                      num_qubits=terms.num_qubits)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        matvec_nocache(x, terms, S, threads=cores)
-    dt = time.perf_counter() - t0
-    return {'value': steps / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': f'{steps} full matvec(s) over the whole workload (D=2^20, 65 groups), '
-                      'complex128, NumPy restatement of apply_h with per-group sort-merge'}
+    matvec_nocache(x, one, wl.S, threads=1)
+    t_one = time.perf_counter() - t0
+    if t_one * J > 20 * budget_s:
+        # very large problem: the single-group timing is the sample, scaled to all groups with
+        # ideal parallel scaling over the cores (an upper bound on the CPU rate)
+        dt = t_one * J / cores
+        return {'value': 1.0 / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                'sample': f'1 of {J} X groups over all D={wl.D} rows on one core '
+                          f'({t_one:.1f} s), scaled to all groups assuming ideal scaling over '
+                          f'{cores} cores; complex128, NumPy restatement of apply_h with '
+                          'per-group sort-merge'}
+    ng = min(J, max(cores, 8))
+    sub = type(terms)(x=terms.x[:ng], z=terms.z[:ng], c=terms.c[:ng], counts=terms.counts[:ng],
+                      num_qubits=terms.num_qubits)
+    t0 = time.perf_counter()
+    matvec_nocache(x, sub, wl.S, threads=cores)
+    t_chunk = time.perf_counter() - t0
+    est_full = t_chunk * J / ng
+    if steps is None:
+        steps = int(budget_s // est_full) if est_full < budget_s else 0
+    if steps >= 1:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            matvec_nocache(x, terms, wl.S, threads=cores)
+        dt = (time.perf_counter() - t0) / steps
+        sample = (f'{steps} full matvec(s) over the whole workload (D={wl.D}, {J} groups), '
+                  'complex128, NumPy restatement of apply_h with per-group sort-merge')
+    else:
+        reps = max(1, int(budget_s // max(t_chunk, 1e-3)))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            matvec_nocache(x, sub, wl.S, threads=cores)
+        dt = (time.perf_counter() - t0) / reps * J / ng
+        sample = (f'{reps} x the first {ng} of {J} X groups over all D={wl.D} rows, scaled '
+                  'linearly to all groups; complex128, NumPy restatement of apply_h')
+    return {'value': 1.0 / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port', 'sample': sample}
 
 
 def run_reference(args, rank, ws):
     if rank != 0:
         return
-    ham, S, xh = workload()
-    # bounded sample: each step is one full matvec (~1-2 s on all host cores)
-    steps = max(1, min(args.steps, 10))
-    for _ in range(min(args.warmup, 1)):
-        cpu_baseline(ham, S, xh, steps=1)
-    cb = cpu_baseline(ham, S, xh, steps=steps)
+    wl = Workload(args.workload, args.rows)
+    # bounded sample sized so that the whole run stays within a few minutes
+    cb = cpu_baseline(wl, budget_s=min(60.0, 6.0 * max(1, args.steps)))
     v = cb['value']
     print(json.dumps({
         'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': ws,
-        'steps': steps, 'warmup': args.warmup, 'ms_per_step': 1e3 / v, 'higher_is_better': True,
-        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128', 'data': 'synthetic',
-        'config': config({'note': 'reference JAX path not installable here (no jax); the '
-                                  'NumPy restatement of its algorithm is timed'}),
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 / v,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128',
+        'data': 'synthetic',
+        'config': wl.config({'note': 'the reference JAX path cannot be installed here (no jax); '
+                                     'the NumPy restatement of its algorithm is timed'}),
         'cpu_baseline': cb,
         'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }), flush=True)
@@ -402,6 +485,11 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--profile', action='store_true',
                     help='run only the timed matvec loop (for ncu captures)')
+    ap.add_argument('--rows', type=int, default=None,
+                    help='override the subspace dimension (profiling captures on a small case)')
+    ap.add_argument('--workload', default='hubbard', choices=['hubbard', 'chemistry', 'random20'],
+                    help='hubbard: Hubbard 4x4, D=2^20 (the headline); chemistry: 64 qubits, '
+                         '50,000 terms, D=2^26; random20: 20 qubits, 200 terms, D=16384')
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == 'ours':
         args.warmup = 3

@@ -91,6 +91,7 @@ typedef struct rq_terms {
     const int32_t  *toff;    /* [J + 1]                                                    */
     const uint64_t *zmask;   /* [K]                                                        */
     const double   *coef;    /* [2K] interleaved (re, im)                                  */
+    const uint32_t *xhash;   /* [J] bucket hash of each X mask (rq_terms_hash), or NULL    */
 } rq_terms_t;
 
 typedef struct rq_operator {
@@ -130,6 +131,10 @@ int rq_xsource(const rq_subspace_t *sub, const uint64_t *xmask, int32_t J, int32
  * zero coefficient.  out is complex double [2D]. */
 int rq_diagonal(const uint64_t *states, int64_t D, const uint64_t *zmask, const double *coef,
                 int32_t K, double *out, void *stream);
+
+/* Fill xhash[j] with the lookup hash of xmask[j] (used by RQ_LOOKUP_HASH matvecs: a row's
+ * target bucket is hash(row) ^ xhash[j]).  Setup call, stream-ordered. */
+int rq_terms_hash(const rq_terms_t *terms, uint32_t *xhash, void *stream);
 
 /* ---- connectivity cache ---------------------------------------------------------------- */
 

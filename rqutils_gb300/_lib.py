@@ -32,7 +32,7 @@ class Subspace(ctypes.Structure):
 class Terms(ctypes.Structure):
     _fields_ = [('J', ctypes.c_int32), ('K', ctypes.c_int32), ('diag_group', ctypes.c_int32),
                 ('is_real', ctypes.c_int32), ('xmask', _c_void_p), ('toff', _c_void_p),
-                ('zmask', _c_void_p), ('coef', _c_void_p)]
+                ('zmask', _c_void_p), ('coef', _c_void_p), ('xhash', _c_void_p)]
 
 
 class Operator(ctypes.Structure):
@@ -68,6 +68,7 @@ SIGNATURES = {
     'rq_xsource': (ctypes.c_int, [_P(Subspace), _c_void_p, ctypes.c_int32, _c_void_p, _c_void_p]),
     'rq_diagonal': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, _c_void_p,
                                    ctypes.c_int32, _c_void_p, _c_void_p]),
+    'rq_terms_hash': (ctypes.c_int, [_P(Terms), _c_void_p, _c_void_p]),
     'rq_conn_build': (ctypes.c_int, [_P(Operator), _c_void_p, _c_void_p, _c_void_p, _c_void_p,
                                      ctypes.c_int32, _P(ctypes.c_int64), _c_void_p, _c_void_p]),
     'rq_matvec': (ctypes.c_int, [_P(Operator), ctypes.c_int32, _c_void_p, _c_void_p, _c_void_p,

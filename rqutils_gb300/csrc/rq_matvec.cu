@@ -150,13 +150,30 @@ __device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, ui
 // ------------------------------------------------------------------------------------------
 // FREE mode with the hash table: the hot kernel
 // ------------------------------------------------------------------------------------------
-// Per row: h(s) once; per group: t = s ^ x_j, sector filter, bucket = (h(s) ^ h(x_j)) >> shift,
-// one 32-byte bucket load.  Four groups are processed per step with their bucket loads issued
-// together.  Keys and the row state use KB-bit arithmetic.
-template <typename V, int KB, bool FILTER>
-__global__ void __launch_bounds__(kThreads, 3)
-k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int gt, int kt,
-              int *err, const int *gate, const int *gate2) {
+// One thread per row.  Per row: h(s) once; per X group: t = s ^ x_j, sector filter,
+// bucket = (h(s) ^ h(x_j)) >> shift, one bucket load.  The per-group data (x_j, h(x_j)) is read
+// with warp-uniform loads that stay in L1, so any number of groups streams without staging;
+// the terms of a group are read from global memory only on a hit.  U bucket loads are issued
+// together; the loop only marks "hot" groups (a key match, a full bucket, or a target equal to
+// the empty key) in a 64-bit mask, resolved once per 64 groups so that the rare divergent work
+// is not interleaved with the probes.
+template <typename R>
+__device__ __forceinline__ cx<R> group_diag(const rq_terms_t &T, int g, uint64_t s);
+
+// Group keys live in shared memory for the whole launch: (x_j, h(x_j)) packed as uint2 for 32-bit
+// keys (8 B per group) or as uint64 + uint32 arrays for 64-bit keys (12 B per group).  Large J
+// runs one 1024-thread block per SM so that up to kMaxResidentGroups fit.
+constexpr int kMaxResidentGroups = 16384;
+
+template <int KB>
+__host__ __device__ inline size_t group_key_bytes(int J) {
+    return KB == 32 ? (size_t)J * 8 : align16((size_t)J * 8) + (size_t)J * 4;
+}
+
+template <typename V, int KB, bool FILTER, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : 4)
+k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int *err,
+              const int *gate, const int *gate2) {
     using R = typename VT<V>::R;
     using K = typename KeyWidth<KB>::K;
     constexpr int NB = KeyWidth<KB>::kNbytes;
@@ -164,29 +181,40 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
     constexpr int U = (KB == 32) ? 8 : 4;  // probes in flight per thread
     if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_g1;
+    __shared__ uint32_t fb[RQ_FILTER_WORDS];
+    __shared__ uint32_t htab[NB * 256];
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
-    uint32_t *fb = reinterpret_cast<uint32_t *>(smem);
-    uint32_t *htab = reinterpret_cast<uint32_t *>(smem + kFilterBytes);
-    const Tile<R> tl = carve<R>(smem + kFilterBytes + NB * 256 * 4, gt, kt);
+    const int J = T.J;
+    // group keys: gk32[j] = (x_j, h_j) for 32-bit keys; gx64[j], gh64[j] for 64-bit keys
+    uint2 *gk32 = reinterpret_cast<uint2 *>(smem);
+    uint64_t *gx64 = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *gh64 = reinterpret_cast<uint32_t *>(smem + align16((size_t)J * 8));
     for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) fb[w] = S.fbits[w];
     init_hash_tables(htab, NB);
+    __syncthreads();
+    for (int j = threadIdx.x; j < J; j += blockDim.x) {
+        const uint64_t xv = T.xmask[j];
+        const uint32_t h = T.xhash ? T.xhash[j] : lin_hash(htab, xv, NB);
+        if (KB == 32) {
+            gk32[j] = make_uint2((uint32_t)xv, h);
+        } else {
+            gx64[j] = xv;
+            gh64[j] = h;
+        }
+    }
+    __syncthreads();
 
     const int64_t D = S.D;
-    const bool d0 = (op.diag0 != nullptr) && (T.diag_group >= 0);
-    const int gstart = (d0 && T.diag_group == 0) ? 1 : 0;
-    const int skip = T.diag_group;
+    const int skip = T.diag_group;  // the x = 0 group is applied outside the probe loop
+    const bool d0 = (op.diag0 != nullptr) && (skip >= 0);
     const K fa = (K)S.fmask_a, fbm = (K)S.fmask_b, empty = (K)S.empty_key;
     const int shift = 32 - S.hbits;
     const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
-    int g1_first = (gstart < T.J) ? load_tile<R>(T, gstart, gt, kt, tl, &s_g1, htab, NB) : T.J;
-    if (g1_first < 0) {
-        if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
-        return;
-    }
-    __syncthreads();  // tables visible even when no tile was loaded
-    const bool resident = (g1_first >= T.J);
+    // Every lane runs the same row batches and super-chunks (lanes past D with nothing to do),
+    // so that the warp can be re-converged after each super-chunk's hot-group resolution; without
+    // the explicit __syncwarp the lanes that took the rare path stay split from the rest for the
+    // remainder of the row.
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < D;
          base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = base + threadIdx.x;
@@ -195,88 +223,76 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
         const K s = (K)s64;
         const uint32_t hs = lin_hash(htab, s64, NB);
         CAcc<R> acc;
+        const cx<R> xi = active ? VT<V>::ld(x, i) : cx<R>{(R)0, (R)0};
         if (active && d0) {
             const R dv = (R)op.diag0[i];
-            const cx<R> xv = VT<V>::ld(x, i);
-            acc.add({dv * xv.re, dv * xv.im});
+            acc.add({dv * xi.re, dv * xi.im});
+        } else if (active && skip >= 0) {
+            acc.add(cmul(group_diag<R>(T, skip, s64), xi));
         }
-        if (!resident && base != (int64_t)blockIdx.x * blockDim.x)
-            g1_first = load_tile<R>(T, gstart, gt, kt, tl, &s_g1, htab, NB);
-        int g0 = gstart, g1 = g1_first;
-        while (g0 < T.J) {
-            if (g1 < 0) {
-                if (err && threadIdx.x == 0) atomicExch(err, RQ_E_RANGE);
-                return;  // uniform across the block
-            }
-            if (active) {
-                if (!d0 && skip >= g0 && skip < g1)
-                    add_group<R>(tl.cf, tl.zm, tl.off[skip - g0], tl.off[skip - g0 + 1], s64,
-                                 VT<V>::ld(x, i), true, acc);
-                // Probe in super-chunks of 64 groups.  The probe loop only marks "hot" groups
-                // (a key match, a full bucket, or a target equal to the empty key) in a 64-bit
-                // mask; the hot groups are resolved afterwards, so the rare divergent work runs
-                // once per super-chunk instead of inside every probe step.
-                for (int gs0 = g0; gs0 < g1; gs0 += 64) {
-                    const int gs1 = min(g1, gs0 + 64);
-                    uint64_t hot = 0ULL;
-                    int g = gs0;
-                    for (; g + U <= gs1; g += U) {
-                        K t[U];
-                        uint32_t b[U];
-                        bool q[U];
-                        typename KeyWidth<KB>::Bucket w[U];
+        for (int gs0 = 0; gs0 < J; gs0 += 64) {
+            const int gs1 = min(J, gs0 + 64);
+            uint64_t hot = 0ULL;
+            int g = gs0;
+            for (; g + U <= gs1; g += U) {
+                K t[U];
+                uint32_t b[U];
+                bool q[U];
+                typename KeyWidth<KB>::Bucket w[U];
 #pragma unroll
-                        for (int u = 0; u < U; ++u) {
-                            const int gl = g + u - g0;
-                            uint32_t hxg;
-                            if (KB == 32) {
-                                const uint2 e = tl.gs[gl];
-                                t[u] = s ^ (K)e.x;
-                                hxg = e.y;
-                            } else {
-                                t[u] = s ^ (K)tl.xm[gl];
-                                hxg = tl.hx[gl];
-                            }
-                            q[u] = (g + u != skip);
-                            if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
-                            b[u] = (hs ^ hxg) >> shift;
-                        }
+                for (int u = 0; u < U; ++u) {
+                    uint32_t hxg;
+                    if (KB == 32) {
+                        const uint2 e = gk32[g + u];
+                        t[u] = s ^ (K)e.x;
+                        hxg = e.y;
+                    } else {
+                        t[u] = s ^ (K)gx64[g + u];
+                        hxg = gh64[g + u];
+                    }
+                    q[u] = active && (g + u != skip);
+                    if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
+                    b[u] = (hs ^ hxg) >> shift;
+                }
 #pragma unroll
-                        for (int u = 0; u < U; ++u)
-                            w[u] = KeyWidth<KB>::load(keys + (size_t)b[u] * kBucketBytes, q[u],
-                                                      S.empty_key);
+                for (int u = 0; u < U; ++u)
+                    w[u] = KeyWidth<KB>::load(keys + (size_t)b[u] * kBucketBytes, q[u],
+                                              S.empty_key);
 #pragma unroll
-                        for (int u = 0; u < U; ++u) {
-                            bool any, open;
-                            test_bucket(w[u], t[u], empty, any, open);
-                            hot |= (uint64_t)(q[u] && (any || !open)) << (g + u - gs0);
-                        }
-                    }
-                    for (; g < gs1; ++g) {  // tail of the super-chunk
-                        const int gl = g - g0;
-                        const K t = s ^ (K)tl.xm[gl];
-                        bool ok = (g != skip);
-                        if (FILTER) ok = ok && sector_ok_k<K>(fb, fa, fbm, t);
-                        if (ok) hot |= 1ULL << (g - gs0);
-                    }
-                    while (hot) {
-                        const int bit = __ffsll((long long)hot) - 1;
-                        hot &= hot - 1ULL;
-                        const int gl = gs0 + bit - g0;
-                        const K t = s ^ (K)tl.xm[gl];
-                        const int m = lookup_hash_at<KB>(S, (uint64_t)t, (hs ^ tl.hx[gl]) >> shift, err);
-                        if (m >= 0)
-                            add_group<R>(tl.cf, tl.zm, tl.off[gl], tl.off[gl + 1], s64,
-                                         VT<V>::ld(x, m), true, acc);
-                    }
+                for (int u = 0; u < U; ++u) {
+                    bool any, open;
+                    test_bucket(w[u], t[u], empty, any, open);
+                    hot |= (uint64_t)(q[u] && (any || !open)) << (g + u - gs0);
                 }
             }
-            if (g1 >= T.J) break;
-            g0 = g1;
-            g1 = load_tile<R>(T, g0, gt, kt, tl, &s_g1, htab, NB);
+            for (; g < gs1; ++g) {  // tail: mark and resolve below
+                const K t = s ^ (KB == 32 ? (K)gk32[g].x : (K)gx64[g]);
+                bool ok = active && (g != skip);
+                if (FILTER) ok = ok && sector_ok_k<K>(fb, fa, fbm, t);
+                if (ok) hot |= 1ULL << (g - gs0);
+            }
+            while (hot) {
+                const int gg = gs0 + __ffsll((long long)hot) - 1;
+                hot &= hot - 1ULL;
+                const uint64_t xv = __ldg(T.xmask + gg);
+                const uint32_t hxg = KB == 32 ? gk32[gg].y : gh64[gg];
+                const int m = lookup_hash_at<KB>(S, s64 ^ xv, (hs ^ hxg) >> shift, err);
+                if (m >= 0) acc.add(cmul(group_diag<R>(T, gg, s64), VT<V>::ld(x, m)));
+            }
+            __syncwarp();
         }
         if (active) VT<V>::st(y, i, acc.get());
     }
+}
+
+// xhash[j] = h(xmask[j])
+template <int KB>
+__global__ void k_terms_hash(const uint64_t *__restrict__ xmask, int J, uint32_t *__restrict__ out) {
+    __shared__ uint32_t htab[KeyWidth<KB>::kNbytes * 256];
+    init_hash_tables(htab, KeyWidth<KB>::kNbytes);
+    __syncthreads();
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < J; j += gridDim.x * blockDim.x)
+        out[j] = lin_hash(htab, xmask[j], KeyWidth<KB>::kNbytes);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -591,23 +607,41 @@ int prepare_launch(KernT kern, size_t smem, size_t &configured, size_t &occ_smem
     return RQ_OK;
 }
 
+template <typename V, int KB, bool FILTER, int BLOCK>
+int launch_hash_block(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
+                      const int *gate, const int *gate2) {
+    auto kern = k_matvec_hash<V, KB, FILTER, BLOCK>;
+    const size_t smem = group_key_bytes<KB>(op.terms.J);
+    static size_t configured = 0, occ_smem = ~size_t(0);
+    static int occ_blocks = 1;
+    if (smem > 48 * 1024 && smem > configured) {
+        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    if (occ_smem != smem) {
+        int per = 0;
+        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, BLOCK, smem));
+        occ_blocks = per < 1 ? 1 : per;
+        occ_smem = smem;
+    }
+    int64_t g = (op.sub.D + BLOCK - 1) / BLOCK;
+    const int64_t cap = (int64_t)sm_count() * occ_blocks;
+    if (g > cap) g = cap;
+    kern<<<(int)(g < 1 ? 1 : g), BLOCK, smem, st>>>(op, static_cast<const V *>(x),
+                                                   static_cast<V *>(y), err, gate, gate2);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}
+
 template <typename V, int KB, bool FILTER>
 int launch_hash(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
                 const int *gate, const int *gate2) {
-    using R = typename VT<V>::R;
-    const rq_terms_t &T = op.terms;
-    const int gt = T.J < kGT ? (T.J > 0 ? T.J : 1) : kGT;
-    const int kt = T.K < kKT ? (T.K > 0 ? T.K : 1) : kKT;
-    const size_t smem = kFilterBytes + KeyWidth<KB>::kNbytes * 256 * 4 + tile_bytes<R>(gt, kt);
-    auto kern = k_matvec_hash<V, KB, FILTER>;
-    static size_t configured = 0, occ_smem = ~size_t(0);
-    static int occ_blocks = 1;
-    int grid = 1;
-    RQ_TRY(prepare_launch(kern, smem, configured, occ_smem, occ_blocks, op.sub.D, grid));
-    kern<<<grid, kThreads, smem, st>>>(op, static_cast<const V *>(x), static_cast<V *>(y), gt, kt,
-                                       err, gate, gate2);
-    RQ_CUDA(cudaGetLastError());
-    return RQ_OK;
+    if (op.terms.J > kMaxResidentGroups)
+        return fail(RQ_E_RANGE, "rq_matvec: more than 16384 X groups for the hash kernel");
+    // small group sets: several 256-thread blocks per SM; large ones: one 1024-thread block
+    if (group_key_bytes<KB>(op.terms.J) <= 16 * 1024)
+        return launch_hash_block<V, KB, FILTER, 256>(op, x, y, err, st, gate, gate2);
+    return launch_hash_block<V, KB, FILTER, 1024>(op, x, y, err, st, gate, gate2);
 }
 
 template <typename V, int LK>
@@ -748,6 +782,18 @@ RQ_API int rq_fullspace_matvec(const rq_terms_t *terms, int32_t n, int32_t vtype
         case RQ_C128: return launch_free<double2, RQ_LOOKUP_IDENTITY>(op, x, y, 0, nullptr, st);
         default: return fail(RQ_E_ARG, "unknown value type");
     }
+}
+
+RQ_API int rq_terms_hash(const rq_terms_t *terms, uint32_t *xhash, void *stream) {
+    if (!terms || !xhash || terms->J < 0 || (terms->J > 0 && !terms->xmask))
+        return fail(RQ_E_ARG, "rq_terms_hash: bad arguments");
+    if (terms->J == 0) return RQ_OK;
+    // the hash is GF(2)-linear over the key bytes; masks below 2^32 hash the same with the
+    // 4-byte and the 8-byte tables, so the 8-byte tables serve both key widths
+    const int grid = (terms->J + kThreads - 1) / kThreads;
+    k_terms_hash<64><<<grid, kThreads, 0, as_stream(stream)>>>(terms->xmask, terms->J, xhash);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
 }
 
 RQ_API int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col, int32_t *grp,

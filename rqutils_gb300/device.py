@@ -127,9 +127,14 @@ class DeviceTerms:
                                   dtype=np.complex128)
         self.coef = torch.from_numpy(cf.view(np.float64)).to(self.device)
         self.group_sizes = np.diff(toff)
+        self.xhash = torch.empty(max(self.J, 1), dtype=torch.int32, device=self.device)
         self.c = L.Terms(J=self.J, K=self.K, diag_group=diag_group, is_real=int(is_real),
                          xmask=L.ptr(self.xmask), toff=L.ptr(self.toff), zmask=L.ptr(self.zmask),
-                         coef=L.ptr(self.coef))
+                         coef=L.ptr(self.coef), xhash=None)
+        if self.J:
+            L.check(L.lib().rq_terms_hash(ctypes.byref(self.c), L.ptr(self.xhash), L.stream_ptr()),
+                    'rq_terms_hash')
+            self.c.xhash = L.ptr(self.xhash)
 
 
 class DeviceOperator:

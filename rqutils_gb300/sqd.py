@@ -58,7 +58,8 @@ def subspace_states(states, num_qubits):
     if a.ndim == 2:
         if a.shape[1] != num_qubits:
             raise ValueError(f'states have {a.shape[1]} columns for {num_qubits} qubits')
-        return np.unique(pack_states(a))
+        from .workloads import sorted_unique
+        return sorted_unique(pack_states(a))
     if a.ndim == 1:
         u = a.astype(np.uint64)
         if len(u) > 1 and not np.all(u[1:] > u[:-1]):
@@ -148,8 +149,9 @@ def hproj(hamiltonian, states, unique_states=False, *, device=None):
         hamiltonian = PauliSumXZ.from_paulisum(hamiltonian, add_padding=True)
     a = np.asarray(states)
     if a.ndim == 2:
+        from .workloads import sorted_unique
         S = pack_states(a)
-        S = np.unique(S) if not unique_states else S
+        S = sorted_unique(S) if not unique_states else S
     else:
         S = a.astype(np.uint64)
     prob = SQDProblem(hamiltonian, S, cache_level=(1, 2), device=device)

@@ -94,92 +94,124 @@ def hubbard_jw(Lx=4, Ly=4, t=1.0, U=4.0, periodic=True):
 
 
 # ----------------------------------------------------------------------------------------------
-# Symplectic products, for the Jordan-Wigner mapping of ladder-operator products
+# Jordan-Wigner mapping of ladder-operator products (symplectic form)
 # ----------------------------------------------------------------------------------------------
 
-def _ladder(p, dagger):
-    """JW ladder operator on qubit p as two (x, z, coeff) Pauli terms:
-    a_p = Z_0..Z_{p-1} (X_p + i Y_p) / 2,  a+_p = Z_0..Z_{p-1} (X_p - i Y_p) / 2,
-    with Y = i X Z in the symplectic form P(x, z) = i^{x.z} X^x Z^z (Hermitian convention)."""
-    chain = (1 << p) - 1
-    xb = 1 << p
-    sgn = -1.0 if dagger else 1.0
-    # X_p: x = xb, z = chain ; i*Y_p: x = xb, z = chain | xb, coefficient i * sgn
-    return [(xb, chain, 0.5 + 0j), (xb, chain | xb, 0.5j * sgn)]
-
-
-def _popcount(a):
-    return bin(a).count('1')
-
-
-def _mul(t1, t2):
-    """Product of Hermitian-convention Pauli terms P(x1,z1) P(x2,z2), both with phase i^{x.z}."""
-    x1, z1, c1 = t1
-    x2, z2, c2 = t2
-    # P(x,z) = i^{|x&z|} X^x Z^z ; X^x1 Z^z1 X^x2 Z^z2 = (-1)^{|z1&x2|} X^{x1^x2} Z^{z1^z2}
-    x, z = x1 ^ x2, z1 ^ z2
-    k = _popcount(x1 & z1) + _popcount(x2 & z2) + 2 * _popcount(z1 & x2) - _popcount(x & z)
-    return (x, z, c1 * c2 * (1j ** (k % 4)))
-
-
-def _label(n, x, z):
-    row = []
-    for col in range(n):
-        q = n - 1 - col
-        xb, zb = (x >> q) & 1, (z >> q) & 1
-        row.append('IXZY'[xb | (zb << 1)] if not (xb and zb) else 'Y')
-    return ''.join(row)
-
-
-def chemistry_jw(n_spatial, rng, keep=None, h_scale=None, g_scale=0.1):
+def chemistry_jw(n_spatial, rng, keep=None, h_scale=None, g_scale=0.1, chunk=1 << 18):
     """Random "chemistry-shaped" Hamiltonian, Jordan-Wigner mapped.
 
-    One-body h_pq ~ N(0, 1/n_spatial) symmetric; two-body (pq|rs) ~ N(0, g_scale^2) with 8-fold
-    symmetry; H = sum_{pq,s} h_pq a+_{ps} a_{qs} + 1/2 sum_{pqrs,s,t} (pq|rs) a+_{ps} a+_{rt} a_{st} a_{qs}.
-    Spin-orbital ordering: qubit p is (p, alpha), qubit n_spatial + p is (p, beta).  The qubit
-    Hamiltonian keeps its ``keep`` largest-|c| Pauli terms (all if None).  Returns ([str], float64).
-    The mapping runs in pure Python over the ladder-operator expansions, so it is meant for small
-    n_spatial in tests; ``chemistry_terms_fast`` handles the benchmark size.
+    One-body h_pq ~ N(0, h_scale^2) symmetric (default h_scale^2 = 1 / n_spatial); two-body
+    (pq|rs) ~ N(0, g_scale^2) with the 8-fold symmetry of real orbitals;
+    H = sum_{pq,s} h_pq a+_{ps} a_{qs} + 1/2 sum_{pqrs,s,t} (pq|rs) a+_{ps} a+_{rt} a_{st} a_{qs}.
+    Spin-orbital ordering: qubit p is (p, alpha), qubit n_spatial + p is (p, beta).  The
+    ladder-operator products are expanded in the symplectic form, vectorised over index tuples
+    and aggregated by sorting; the ``keep`` largest-|c| Pauli terms are returned (all if None).
+    Returns ([str], float64).
     """
     ns = n_spatial
     n = 2 * ns
+    if n > 64:
+        raise ValueError('at most 32 spatial orbitals (64 qubits)')
     if h_scale is None:
         h_scale = 1.0 / np.sqrt(ns)
     h = rng.normal(0., h_scale, size=(ns, ns))
     h = 0.5 * (h + h.T)
     g = _random_eri(rng, ns, g_scale)
-    acc = {}
+    acc_x, acc_z, acc_c = [], [], []
 
-    def add_product(ops, coeff):
-        terms = [(0, 0, complex(coeff))]
-        for (p, dag) in ops:
-            terms = [_mul(a, b) for a in terms for b in _ladder(p, dag)]
-        for (x, z, c) in terms:
-            acc[(x, z)] = acc.get((x, z), 0) + c
+    def flush(xs, zs, cs):
+        x, z, c = _aggregate(np.concatenate(xs), np.concatenate(zs), np.concatenate(cs))
+        acc_x.append(x)
+        acc_z.append(z)
+        acc_c.append(c)
 
-    for s in (0, ns):
-        for p in range(ns):
-            for q in range(ns):
-                if h[p, q] != 0:
-                    add_product([(p + s, True), (q + s, False)], h[p, q])
-    for s in (0, ns):
-        for t in (0, ns):
-            for p in range(ns):
-                for q in range(ns):
-                    for r in range(ns):
-                        for u in range(ns):
-                            if p + s == r + t or q + s == u + t:
-                                continue
-                            add_product([(p + s, True), (r + t, True), (u + t, False),
-                                         (q + s, False)], 0.5 * g[p, q, r, u])
-    items = [(k, v) for k, v in acc.items() if abs(v) > 1e-14]
-    # Hermitian-convention coefficients of a Hermitian operator are real
-    labels = [_label(n, x, z) for (x, z), _ in items]
-    coeffs = np.array([v.real for _, v in items])
-    order = np.argsort(-np.abs(coeffs), kind='stable')
+    # one-body: a+_p a_q within a spin block
+    pp, qq = np.meshgrid(np.arange(ns), np.arange(ns), indexing='ij')
+    pp, qq = pp.ravel(), qq.ravel()
+    cf = h[pp, qq]
+    xs, zs, cs = [], [], []
+    for off in (0, ns):
+        x, z, c = _ladder_product([(pp + off, True), (qq + off, False)], cf)
+        xs.append(x), zs.append(z), cs.append(c)
+    flush(xs, zs, cs)
+    # two-body: 1/2 (pq|rs) a+_{p s} a+_{r t} a_{s t} a_{q s}
+    idx = np.arange(ns ** 4)
+    P, Q, Rr, Ss = np.unravel_index(idx, (ns, ns, ns, ns))
+    G = 0.5 * g[P, Q, Rr, Ss]
+    for so in (0, ns):
+        for to in (0, ns):
+            a, b, cc, d = P + so, Rr + to, Ss + to, Q + so
+            ok = (a != b) & (cc != d)
+            a, b, cc, d, Gk = a[ok], b[ok], cc[ok], d[ok], G[ok]
+            for lo in range(0, len(a), chunk):
+                sl = slice(lo, lo + chunk)
+                x, z, c = _ladder_product([(a[sl], True), (b[sl], True), (cc[sl], False),
+                                           (d[sl], False)], Gk[sl])
+                flush([x], [z], [c])
+    x, z, c = _aggregate(np.concatenate(acc_x), np.concatenate(acc_z), np.concatenate(acc_c))
+    # Hermitian operator: the Pauli coefficients are real up to round-off
+    c = c.real
+    nz = np.abs(c) > 1e-13
+    x, z, c = x[nz], z[nz], c[nz]
+    order = np.argsort(-np.abs(c), kind='stable')
     if keep is not None:
         order = order[:keep]
-    return [labels[i] for i in order], coeffs[order]
+    return xz_labels(x[order], z[order], n), c[order]
+
+
+def _popcount64(a):
+    return np.bitwise_count(a).astype(np.int64)
+
+
+def _ladder_product(ops, coeff):
+    """Expand prod_k (ladder op k) * coeff for arrays of tuples.  Ladder operators on qubit p:
+    a_p = Z_0..Z_{p-1} (X_p + i Y_p) / 2, a+_p = Z_0..Z_{p-1} (X_p - i Y_p) / 2, written with
+    Hermitian Pauli strings P(x, z) = i^{|x & z|} X^x Z^z.  Returns flat (x, z, c) arrays."""
+    one = np.uint64(1)
+    x = np.zeros((len(coeff), 1), dtype=np.uint64)
+    z = np.zeros((len(coeff), 1), dtype=np.uint64)
+    c = np.asarray(coeff, dtype=np.complex128)[:, None]
+    for p, dagger in ops:
+        p = np.asarray(p, dtype=np.uint64)
+        xb = one << p
+        chain = xb - one
+        # the two terms of the ladder operator: (xb, chain, 1/2) and (xb, chain|xb, +-i/2)
+        tx = np.stack([xb, xb], axis=1)
+        tz = np.stack([chain, chain | xb], axis=1)
+        tc = np.array([0.5, (-0.5j if dagger else 0.5j)])
+        X1, Z1 = x[:, :, None], z[:, :, None]
+        X2, Z2 = tx[:, None, :], tz[:, None, :]
+        Xn, Zn = X1 ^ X2, Z1 ^ Z2
+        k = (_popcount64(X1 & Z1) + _popcount64(X2 & Z2) + 2 * _popcount64(Z1 & X2)
+             - _popcount64(Xn & Zn)) & 3
+        ph = np.array([1, 1j, -1, -1j])[k]
+        c = (c[:, :, None] * tc[None, None, :] * ph).reshape(len(c), -1)
+        x = Xn.reshape(len(c), -1)
+        z = Zn.reshape(len(c), -1)
+    return x.ravel(), z.ravel(), c.ravel()
+
+
+def _aggregate(x, z, c):
+    """Sum coefficients of equal (x, z) strings (sorted by (x, z))."""
+    if len(x) == 0:
+        return x, z, c
+    order = np.lexsort((z, x))
+    x, z, c = x[order], z[order], c[order]
+    start = np.concatenate([[True], (x[1:] != x[:-1]) | (z[1:] != z[:-1])])
+    idx = np.nonzero(start)[0]
+    return x[idx], z[idx], np.add.reduceat(c, idx)
+
+
+def xz_labels(x, z, n):
+    """Pauli labels of (x, z) masks; character 0 is qubit n-1."""
+    x = np.asarray(x, dtype=np.uint64)
+    z = np.asarray(z, dtype=np.uint64)
+    shifts = np.arange(n - 1, -1, -1, dtype=np.uint64)
+    xb = ((x[:, None] >> shifts) & np.uint64(1)).astype(np.uint8)
+    zb = ((z[:, None] >> shifts) & np.uint64(1)).astype(np.uint8)
+    code = xb + 2 * zb  # I=0, X=1, Z=2, Y=3
+    chars = np.array([ord('I'), ord('X'), ord('Z'), ord('Y')], dtype=np.uint32)[code]
+    return [s for s in np.ascontiguousarray(chars).view(f'<U{n}').ravel()]
 
 
 def _random_eri(rng, ns, scale):
@@ -242,11 +274,22 @@ def sample_sector(rng, D, blocks):
         for nb, w in blocks:
             words |= _fixed_weight_words(rng, nb, w, need) << np.uint64(shift)
             shift += nb
-        have = np.unique(np.concatenate([have, words]))
-    # drop a uniformly chosen surplus
+        have = sorted_unique(np.concatenate([have, words]))
+    # drop a uniformly chosen surplus (keeps the array sorted)
     if len(have) > D:
-        have = np.sort(rng.choice(have, size=D, replace=False))
+        have = np.delete(have, rng.choice(len(have), size=len(have) - D, replace=False))
     return have
+
+
+def sorted_unique(a):
+    """Sorted distinct values of a 1-d array (sort + adjacent difference)."""
+    a = np.sort(np.asarray(a))
+    if len(a) == 0:
+        return a
+    keep = np.empty(len(a), dtype=bool)
+    keep[0] = True
+    np.not_equal(a[1:], a[:-1], out=keep[1:])
+    return a[keep]
 
 
 def _enumerate_sector(blocks):

@@ -197,3 +197,55 @@ def test_extreme_keys_and_empty_choice():
     from oracle.sqd import xsource_search
     for j, x in enumerate([0, 1, 2 ** 64 - 1, 5]):
         np.testing.assert_array_equal(xs[j], xsource_search(S, x))
+
+
+@pytest.mark.parametrize('name', ['notebook', 'local20', 'n16dense'])
+def test_key_widths_agree(name):
+    """Forced 64-bit keys on problems that also fit 32-bit keys give the same tables."""
+    from rqutils_gb300.device import DeviceSubspace
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    from rqutils_gb300.sqd import subspace_states
+    case = load(name)
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        h = PauliSumXZ.from_paulisum(hamiltonian(case), force_real=True)
+    S = subspace_states(case['states'], h.num_qubits)
+    a = DeviceSubspace(S, num_qubits=h.num_qubits, key_bits=32).xsource(h.xmask).cpu().numpy()
+    b = DeviceSubspace(S, num_qubits=h.num_qubits, key_bits=64).xsource(h.xmask).cpu().numpy()
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, case['xsources'][:, :int(case['D'])])
+
+
+@pytest.fixture(scope='module')
+def chem40():
+    """40-qubit chemistry-shaped problem (64-bit keys): 20 spatial orbitals, 3000 terms,
+    20000 states at 10 alpha + 10 beta electrons."""
+    from rqutils_gb300 import workloads
+    from oracle.paulis import from_paulisum as oterms
+    from oracle import sqd as osqd
+    rng = np.random.default_rng(21)
+    labels, coeffs = workloads.chemistry_jw(20, rng, keep=3000)
+    S = workloads.sample_sector(rng, 20000, [(20, 10), (20, 10)])
+    t = oterms((labels, coeffs), force_real=True)
+    xs = np.stack([osqd.xsource_search(S, xv) for xv in t.x])
+    v = workloads.random_vector(rng, len(S))
+    ref = osqd.matvec_xcached(v, xs, t, S)
+    return labels, coeffs, S, v, ref, xs
+
+
+@pytest.mark.parametrize('cache_level', [(0, 0), (1, 0), (1, 2)])
+@pytest.mark.parametrize('lookup', ['hash', 'bsearch'])
+def test_chemistry_64bit_matvec(chem40, cache_level, lookup):
+    import torch
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    from rqutils_gb300.sqd import SQDProblem
+    labels, coeffs, S, v, ref, xs = chem40
+    h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
+    prob = SQDProblem(h, S, cache_level=cache_level, lookup=lookup)
+    assert prob.sub.key_bits == 64
+    y = prob.op.matvec(torch.as_tensor(v).cuda()).cpu().numpy()
+    assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref)
+    y32 = prob.op.matvec(torch.as_tensor(v).to(torch.complex64).cuda()).cpu().numpy()
+    assert np.linalg.norm(y32 - ref) <= 1e-6 * np.linalg.norm(ref)
+    got = prob.sub.xsource(h.xmask).cpu().numpy()
+    np.testing.assert_array_equal(got, xs)

@@ -101,3 +101,52 @@ def test_hubbard_matches_dense_small():
     idx = [i for i in range(16) if bin(i & 0b11).count('1') == 1 and bin(i >> 2).count('1') == 1]
     w = np.linalg.eigvalsh(H[np.ix_(idx, idx)])
     assert abs(w[0] - (4 - np.sqrt(16 + 16)) / 2) < 1e-12
+
+
+def _jw_matrices(n):
+    """a_p as explicit matrices: Z on qubits below p, |0><1| on p (character 0 = qubit n-1)."""
+    I2, Z = np.eye(2), np.diag([1., -1.])
+    lower = np.array([[0, 1], [0, 0]], dtype=complex)
+    ops = []
+    for p in range(n):
+        m = np.ones((1, 1))
+        for q in range(n - 1, -1, -1):
+            m = np.kron(m, Z if q < p else (lower if q == p else I2))
+        ops.append(m)
+    return ops
+
+
+@pytest.mark.parametrize('ns', [1, 2, 3])
+def test_chemistry_jw_matches_fermion_matrices(ns):
+    """The vectorised Jordan-Wigner mapping equals the second-quantised operator built from
+    explicit ladder matrices."""
+    from oracle import dense
+    labels, coeffs = workloads.chemistry_jw(ns, np.random.default_rng(5))
+    H = dense.hamiltonian_matrix(labels, coeffs)
+    rng = np.random.default_rng(5)
+    h = rng.normal(0, 1 / np.sqrt(ns), size=(ns, ns))
+    h = 0.5 * (h + h.T)
+    g = workloads._random_eri(rng, ns, 0.1)
+    n = 2 * ns
+    a = _jw_matrices(n)
+    ad = [m.conj().T for m in a]
+    ref = np.zeros((2 ** n,) * 2, dtype=complex)
+    for s in (0, ns):
+        for p in range(ns):
+            for q in range(ns):
+                ref += h[p, q] * ad[p + s] @ a[q + s]
+    for s in (0, ns):
+        for t in (0, ns):
+            for p in range(ns):
+                for q in range(ns):
+                    for r in range(ns):
+                        for u in range(ns):
+                            ref += 0.5 * g[p, q, r, u] * ad[p + s] @ ad[r + t] @ a[u + t] @ a[q + s]
+    np.testing.assert_allclose(H, ref, atol=1e-13)
+
+
+def test_chemistry_truncation_keeps_largest():
+    labels, coeffs = workloads.chemistry_jw(4, np.random.default_rng(1), keep=50)
+    full_l, full_c = workloads.chemistry_jw(4, np.random.default_rng(1))
+    assert len(labels) == 50
+    assert np.min(np.abs(coeffs)) >= np.sort(np.abs(full_c))[-50] - 1e-15
