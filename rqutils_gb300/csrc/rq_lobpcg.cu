@@ -16,8 +16,10 @@
 // Mixed precision runs a 32-bit phase first and continues in the 64-bit type from its x and y.
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "rq_common.cuh"
@@ -120,8 +122,92 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 #define GATE(st) \
     if ((st)->active == 0) return;
 
-#define GRID_LOOP(i, D) \
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (D); i += (int64_t)gridDim.x * blockDim.x)
+// ------------------------------------------------------------------------------------------
+// segment policies: which rows a block handles and where its sums go
+// ------------------------------------------------------------------------------------------
+
+// One problem: grid-stride over [0, D), deterministic grid reduction into the state.
+struct SegOne {
+    State *st;
+    int64_t D;
+    void *red;
+    __device__ __forceinline__ State *state() const { return st; }
+    __device__ __forceinline__ int64_t begin() const {
+        return blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    }
+    __device__ __forceinline__ int64_t end() const { return D; }
+    __device__ __forceinline__ int64_t stride() const { return (int64_t)gridDim.x * blockDim.x; }
+    template <int NV>
+    __device__ void reduce(double2 (&v)[NV], int slot) const {
+        grid_reduce<NV>(v, red, st->red + slot);
+    }
+};
+
+// Many problems: block c handles chunk c, rows [crow[c], crow[c + 1]) of problem cprob[c];
+// problem p owns chunks [cofs[p], cofs[p + 1]).  Sums: each block writes its partials; the last
+// block of a problem (per-problem counter) adds that problem's partials in chunk order.
+struct SegBatch {
+    State *states;
+    const int32_t *cprob;
+    const int64_t *crow;
+    const int32_t *cofs;
+    double2 *part;          // [nchunks * kMaxReduce]
+    unsigned int *counter;  // [P]
+    __device__ __forceinline__ State *state() const { return states + cprob[blockIdx.x]; }
+    __device__ __forceinline__ int64_t begin() const { return crow[blockIdx.x] + threadIdx.x; }
+    __device__ __forceinline__ int64_t end() const { return crow[blockIdx.x + 1]; }
+    __device__ __forceinline__ int64_t stride() const { return blockDim.x; }
+    template <int NV>
+    __device__ void reduce(double2 (&v)[NV], int slot) const {
+        __shared__ double2 red[kThreads / 32][NV];
+        __shared__ bool last;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int nwarp = (blockDim.x + 31) >> 5;
+        const int c = blockIdx.x, p = cprob[c];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                v[k].x += __shfl_xor_sync(0xffffffffu, v[k].x, o);
+                v[k].y += __shfl_xor_sync(0xffffffffu, v[k].y, o);
+            }
+            if (lane == 0) red[warp][k] = v[k];
+        }
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                double2 a = (lane < nwarp) ? red[lane][k] : make_double2(0., 0.);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+                    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+                }
+                if (lane == 0) part[(size_t)c * kMaxReduce + k] = a;
+            }
+            if (lane == 0) {
+                __threadfence();
+                const unsigned int n = (unsigned int)(cofs[p + 1] - cofs[p]);
+                last = (atomicAdd(counter + p, 1u) == n - 1);
+            }
+        }
+        __syncthreads();
+        if (!last) return;
+        __threadfence();
+        if (threadIdx.x < NV) {  // chunk order: deterministic
+            double2 a = make_double2(0., 0.);
+            for (int cc = cofs[p]; cc < cofs[p + 1]; ++cc) {
+                const double2 q = __ldcg(part + (size_t)cc * kMaxReduce + threadIdx.x);
+                a.x += q.x;
+                a.y += q.y;
+            }
+            states[p].red[slot + threadIdx.x] = a;
+        }
+        if (threadIdx.x == 0) counter[p] = 0u;
+    }
+};
+
+#define SEG_LOOP(i) for (int64_t i = seg.begin(); i < seg.end(); i += seg.stride())
 
 // ------------------------------------------------------------------------------------------
 // vector kernels (one pass each)
@@ -134,13 +220,14 @@ struct Pairs {
     const V *b[NP];
 };
 
-template <typename V, int NP>
+template <typename V, int NP, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_dots(State *st, int64_t D, Pairs<V, NP> pr, int slot, void *red) {
+k_dots(SEG seg, Pairs<V, NP> pr, int slot) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     CDot<R> acc[NP];
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
 #pragma unroll
         for (int k = 0; k < NP; ++k)
             acc[k].add(VT<V>::ld(pr.a[k], i), VT<V>::ld(pr.b[k], i), VT<V>::kComplex);
@@ -148,52 +235,55 @@ k_dots(State *st, int64_t D, Pairs<V, NP> pr, int slot, void *red) {
     double2 v[NP];
 #pragma unroll
     for (int k = 0; k < NP; ++k) v[k] = acc[k].get();
-    grid_reduce<NP>(v, red, st->red + slot);
+    seg.template reduce<NP>(v, slot);
 }
 
 // out = v * scale where scale = 1 / sqrt(red[nslot].x) (1 when that is 0); optional <x,out>, <y,out>
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_normalize(State *st, int64_t D, const V *in, V *out, int nslot) {
+k_normalize(SEG seg, const V *in, V *out, int nslot) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const double n = sqrt(st->red[nslot].x);
     const R inv = (R)(n == 0. ? 1. : 1. / n);
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         cx<R> v = VT<V>::ld(in, i);
         VT<V>::st(out, i, {v.re * inv, v.im * inv});
     }
 }
 
 // v <- v - x ip0 - y ip1 (ip from red[kIp0], red[kIp1]); red[kVn] = |v|^2
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_sub2_norm(State *st, int64_t D, const V *x, const V *y, V *v, void *red) {
+k_sub2_norm(SEG seg, const V *x, const V *y, V *v) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const cx<R> m0 = c_of<R>(make_double2(-st->red[kIp0].x, -st->red[kIp0].y));
     const cx<R> m1 = c_of<R>(make_double2(-st->red[kIp1].x, -st->red[kIp1].y));
     CDot<R> nn;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         cx<R> w = axpy(m0, VT<V>::ld(x, i), VT<V>::ld(v, i));
         w = axpy(m1, VT<V>::ld(y, i), w);
         VT<V>::st(v, i, w);
         nn.add(w, w, VT<V>::kComplex);
     }
     double2 r[1] = {nn.get()};
-    grid_reduce<1>(r, red, st->red + kVn);
+    seg.template reduce<1>(r, kVn);
 }
 
 // v <- v / (|v| or 1); red[kIp0] = <x, v>, red[kIp1] = <y, v>
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_scale_dots2(State *st, int64_t D, const V *x, const V *y, V *v, int do_scale, void *red) {
+k_scale_dots2(SEG seg, const V *x, const V *y, V *v, int do_scale) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const double n = sqrt(st->red[kVn].x);
     const R inv = (R)((!do_scale || n == 0.) ? 1. : 1. / n);
     CDot<R> d0, d1;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         cx<R> w = VT<V>::ld(v, i);
         w = {w.re * inv, w.im * inv};
         if (do_scale) VT<V>::st(v, i, w);
@@ -201,31 +291,34 @@ k_scale_dots2(State *st, int64_t D, const V *x, const V *y, V *v, int do_scale, 
         d1.add(VT<V>::ld(y, i), w, VT<V>::kComplex);
     }
     double2 r[2] = {d0.get(), d1.get()};
-    grid_reduce<2>(r, red, st->red + kIp0);
+    seg.template reduce<2>(r, kIp0);
 }
 
 // p = v if |v| >= 0.99 else 0 (ground_locg.py:421)
-template <typename V>
-__global__ void __launch_bounds__(kThreads) k_mask(State *st, int64_t D, const V *v, V *p) {
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_mask(SEG seg, const V *v, V *p) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const R m = (R)(sqrt(st->red[kVn].x) >= 0.99 ? 1. : 0.);
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         cx<R> w = VT<V>::ld(v, i);
         VT<V>::st(p, i, {w.re * m, w.im * m});
     }
 }
 
 // Gram entries of (x, y, p): <y,Ax> <p,Ax> <p,Ay> <x,Ax> <y,Ay> <p,Ap>
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_gram3(State *st, int64_t D, const V *x, const V *y, const V *p, const V *ax, const V *ay,
-        const V *ap, void *red) {
+k_gram3(SEG seg, const V *x, const V *y, const V *p, const V *ax, const V *ay,
+        const V *ap) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     CDot<R> g[6];
     const bool c = VT<V>::kComplex;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i), yi = VT<V>::ld(y, i), pi = VT<V>::ld(p, i);
         const cx<R> axi = VT<V>::ld(ax, i), ayi = VT<V>::ld(ay, i), api = VT<V>::ld(ap, i);
         g[0].add(yi, axi, c);
@@ -238,18 +331,19 @@ k_gram3(State *st, int64_t D, const V *x, const V *y, const V *p, const V *ax, c
     double2 r[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) r[k] = g[k].get();
-    grid_reduce<6>(r, red, st->red + kG10);
+    seg.template reduce<6>(r, kG10);
 }
 
 // Gram entries of (x, p) for the first Rayleigh-Ritz step: <p,Ax> <x,Ax> <p,Ap>
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_gram2(State *st, int64_t D, const V *x, const V *p, const V *ax, const V *ap, void *red) {
+k_gram2(SEG seg, const V *x, const V *p, const V *ax, const V *ap) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     CDot<R> g[3];
     const bool c = VT<V>::kComplex;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
         const cx<R> axi = VT<V>::ld(ax, i), api = VT<V>::ld(ap, i);
         g[0].add(pi, axi, c);
@@ -257,29 +351,31 @@ k_gram2(State *st, int64_t D, const V *x, const V *p, const V *ax, const V *ap, 
         g[2].add(pi, api, c);
     }
     double2 r[3] = {g[0].get(), g[1].get(), g[2].get()};
-    grid_reduce<3>(r, red, st->red + kG10);
+    seg.template reduce<3>(r, kG10);
 }
 
 // s = k1 y + k2 p: red[kSn] = |s|^2
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_upd_s(State *st, int64_t D, const V *y, const V *p, void *red) {
+k_upd_s(SEG seg, const V *y, const V *p) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const cx<R> k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
     CDot<R> nn;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
         nn.add(s, s, VT<V>::kComplex);
     }
     double2 r[1] = {nn.get()};
-    grid_reduce<1>(r, red, st->red + kSn);
+    seg.template reduce<1>(r, kSn);
 }
 
 // t = s (k0/|s|) - x |s|, u = k0 x + s: red[kTn] = |t|^2, red[kUn] = |u|^2
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_upd_tu(State *st, int64_t D, const V *x, const V *y, const V *p, void *red) {
+k_upd_tu(SEG seg, const V *x, const V *y, const V *p) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const double ns = sqrt(st->red[kSn].x);
@@ -288,7 +384,7 @@ k_upd_tu(State *st, int64_t D, const V *x, const V *y, const V *p, void *red) {
     const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
     const cx<R> mns = {(R)(-ns), (R)0};
     CDot<R> tn, un;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i);
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
         const cx<R> t = keep_y ? VT<V>::ld(y, i) : axpy(mns, xi, cmul(k0s, s));
@@ -297,13 +393,14 @@ k_upd_tu(State *st, int64_t D, const V *x, const V *y, const V *p, void *red) {
         un.add(u, u, VT<V>::kComplex);
     }
     double2 r[2] = {tn.get(), un.get()};
-    grid_reduce<2>(r, red, st->red + kTn);
+    seg.template reduce<2>(r, kTn);
 }
 
 // x <- u / |u|, y <- t / |t|; FAST also carries A x, A y by the same combinations.
-template <typename V, bool CARRY>
+template <typename V, bool CARRY, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_upd_xy(State *st, int64_t D, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
+k_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const double ns = sqrt(st->red[kSn].x);
@@ -313,7 +410,7 @@ k_upd_xy(State *st, int64_t D, V *x, V *y, const V *p, V *ax, V *ay, const V *ap
     const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
     const cx<R> mns = {(R)(-ns), (R)0};
     const R rit = (R)it, riu = (R)iu;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i);
         const cx<R> yi = VT<V>::ld(y, i);
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, yi));
@@ -334,15 +431,16 @@ k_upd_xy(State *st, int64_t D, V *x, V *y, const V *p, V *ax, V *ay, const V *ap
 }
 
 // iteration 1 update (ground_locg.py:278-281): t = p k0 - x k1, u = x k0 + p k1 -> norms
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_upd2_norms(State *st, int64_t D, const V *x, const V *p, void *red) {
+k_upd2_norms(SEG seg, const V *x, const V *p) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]);
     const cx<R> mk1 = {-k1.re, -k1.im};
     CDot<R> tn, un;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
         const cx<R> t = axpy(mk1, xi, cmul(k0, pi));
         const cx<R> u = axpy(k1, pi, cmul(k0, xi));
@@ -350,18 +448,19 @@ k_upd2_norms(State *st, int64_t D, const V *x, const V *p, void *red) {
         un.add(u, u, VT<V>::kComplex);
     }
     double2 r[2] = {tn.get(), un.get()};
-    grid_reduce<2>(r, red, st->red + kTn);
+    seg.template reduce<2>(r, kTn);
 }
 
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_upd2_xy(State *st, int64_t D, V *x, V *y, const V *p) {
+k_upd2_xy(SEG seg, V *x, V *y, const V *p) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]);
     const cx<R> mk1 = {-k1.re, -k1.im};
     const R rit = (R)(1. / sqrt(st->red[kTn].x)), riu = (R)(1. / sqrt(st->red[kUn].x));
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
         const cx<R> t = axpy(mk1, xi, cmul(k0, pi));
         const cx<R> u = axpy(k1, pi, cmul(k0, xi));
@@ -372,15 +471,16 @@ k_upd2_xy(State *st, int64_t D, V *x, V *y, const V *p) {
 
 // r = Ax - theta x; red[kAxn] = |Ax|^2, red[kRn] = |r|^2.  theta from st->theta, or from
 // Re red[kMisc] (iteration 0: rho = Re <x, Ax>) when use_rho.
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_resid(State *st, int64_t D, const V *ax, const V *x, V *r, int use_rho, void *red) {
+k_resid(SEG seg, const V *ax, const V *x, V *r, int use_rho) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const double th = use_rho ? st->red[kMisc].x : st->theta;
     const cx<R> mth = {(R)(-th), (R)0};
     CDot<R> an, rn;
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         const cx<R> a = VT<V>::ld(ax, i);
         const cx<R> w = axpy(mth, VT<V>::ld(x, i), a);
         VT<V>::st(r, i, w);
@@ -388,18 +488,19 @@ k_resid(State *st, int64_t D, const V *ax, const V *x, V *r, int use_rho, void *
         rn.add(w, w, VT<V>::kComplex);
     }
     double2 out[2] = {an.get(), rn.get()};
-    grid_reduce<2>(out, red, st->red + kAxn);
+    seg.template reduce<2>(out, kAxn);
 }
 
 // w = r / (d - theta), |d - theta| floored at 1e-8 (1 + |theta|): the Jacobi preconditioner.
-template <typename V>
+template <typename V, typename SEG>
 __global__ void __launch_bounds__(kThreads)
-k_jacobi(State *st, int64_t D, const double *diag, const V *r, V *w) {
+k_jacobi(SEG seg, const double *diag, const V *r, V *w) {
+    State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
     const double th = st->theta;
     const double floor_ = 1e-8 * (1. + fabs(th));
-    GRID_LOOP(i, D) {
+    SEG_LOOP(i) {
         double den = diag[i] - th;
         if (fabs(den) < floor_) den = den < 0 ? -floor_ : floor_;
         const R f = (R)(1. / den);
@@ -412,21 +513,20 @@ template <typename VS, typename VD>
 __global__ void __launch_bounds__(kThreads) k_convert(int64_t D, const VS *a, VD *b) {
     using RS = typename VT<VS>::R;
     using RD = typename VT<VD>::R;
-    GRID_LOOP(i, D) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
+         i += (int64_t)gridDim.x * blockDim.x) {
         const cx<RS> v = VT<VS>::ld(a, i);
         VT<VD>::st(b, i, {(RD)v.re, (RD)v.im});
     }
 }
 
-template <typename V>
-__global__ void __launch_bounds__(kThreads) k_copy(State *st, int64_t D, const V *a, V *b) {
-    GATE(st);
-    GRID_LOOP(i, D) b[i] = a[i];
-}
-
 // ------------------------------------------------------------------------------------------
-// scalar kernels (one thread)
+// scalar kernels: one thread per problem
 // ------------------------------------------------------------------------------------------
+#define FOR_ACTIVE_PROBLEMS(states, P, st)                                          \
+    for (int p_ = blockIdx.x * blockDim.x + threadIdx.x; p_ < (P);              \
+         p_ += gridDim.x * blockDim.x)                                             \
+        for (State *st = (states) + p_; st != nullptr && st->active; st = nullptr)
 
 // Lowest eigenpair of a Hermitian 3x3 given by its strict lower triangle (m10, m20, m21) and its
 // diagonal (complex values, real part used as in ground_locg.py:446); Cardano (Kopp 2008).
@@ -500,19 +600,21 @@ __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2
     for (int k = 0; k < 3; ++k) v[k] = make_double2(c[k].x / nrm, c[k].y / nrm);
 }
 
-__global__ void k_rr3(State *st) {
-    GATE(st);
-    double lam;
-    double2 v[3];
-    eig3(st->red[kG10], st->red[kG20], st->red[kG21], st->red[kG00], st->red[kG11], st->red[kG22],
-         lam, v, st->guard != 0);
-    st->theta = lam;
-    for (int k = 0; k < 3; ++k) st->kappa[k] = v[k];
+__global__ void k_rr3(State *states, int P) {
+    FOR_ACTIVE_PROBLEMS(states, P, st) {
+        double lam;
+        double2 v[3];
+        eig3(st->red[kG10], st->red[kG20], st->red[kG21], st->red[kG00], st->red[kG11],
+             st->red[kG22], lam, v, st->guard != 0);
+        st->theta = lam;
+        for (int k = 0; k < 3; ++k) st->kappa[k] = v[k];
+        break;
+    }
 }
 
 // eigenpair_2x2 (ground_locg.py:424-435) of [[g00, conj(g10)], [g10, g11]]
-__global__ void k_rr2(State *st) {
-    GATE(st);
+__global__ void k_rr2(State *states, int P) {
+    FOR_ACTIVE_PROBLEMS(states, P, st) {
     // k_gram2 wrote <p,Ax>, <x,Ax>, <p,Ap> to three consecutive slots from kG10
     const double2 m10 = st->red[kG10];
     const double d0 = st->red[kG10 + 1].x;  // <x, Ax>
@@ -528,13 +630,16 @@ __global__ void k_rr2(State *st) {
     st->kappa[0] = make_double2(v0.x / n, v0.y / n);
     st->kappa[1] = make_double2(-1. / n, 0.);
     st->kappa[2] = make_double2(0., 0.);
+    break;
+    }
 }
 
 // iteration 0: rho = Re <x, Ax> into red[kMisc] (already there from k_dots); nothing else.
 
-// Convergence test of ground_locg.py:329-334 and phase bookkeeping.
-__global__ void k_check(State *st) {
-    GATE(st);
+// Convergence test of ground_locg.py:329-334 and phase bookkeeping; a problem that stops
+// decrements the count of active problems.
+__global__ void k_check(State *states, int P, int *nactive) {
+    FOR_ACTIVE_PROBLEMS(states, P, st) {
     const double rn = sqrt(st->red[kRn].x);
     const double an = sqrt(st->red[kAxn].x);
     const double th = st->theta;
@@ -572,15 +677,22 @@ __global__ void k_check(State *st) {
         }
     }
     st->converged = conv ? 1 : 0;
-    if (conv || st->iter >= st->maxiter) st->active = 0;
+    if (conv || st->iter >= st->maxiter) {
+        st->active = 0;
+        atomicSub(nactive, 1);
+    }
+    break;
+    }
 }
 
 // FAST: a refresh starts -- reset the counter (runs only when want_refresh is set)
-__global__ void k_refresh_mark(State *st) {
-    GATE(st);
-    if (st->want_refresh) {
-        st->since_refresh = 0;
-        st->matvecs += 2;
+__global__ void k_refresh_mark(State *states, int P) {
+    FOR_ACTIVE_PROBLEMS(states, P, st) {
+        if (st->want_refresh) {
+            st->since_refresh = 0;
+            st->matvecs += 2;
+        }
+        break;
     }
 }
 
@@ -646,51 +758,67 @@ Vecs<V> carve_vecs(char *base, size_t bytes) {
     return v;
 }
 
-template <typename V>
-struct Phase {
-    rq_matvec_fn fn;  // caller-supplied matvec, or null for the operator's own kernels
-    void *ctx;
+// Matvec of a phase: the operator's own kernels gated by the problem's flags, or a caller
+// callback.  `refresh` marks the FAST variant's gated recomputation of A x, A y.
+struct MvOne {
     const rq_operator_t *op;
+    void *scratch;
+    int operator()(int32_t vt, const void *in, void *out, cudaStream_t s, State *states,
+                   bool refresh) const {
+        return matvec_dispatch(*op, vt, in, out, scratch, s, &states->active,
+                               refresh ? &states->want_refresh : nullptr);
+    }
+};
+
+struct MvCallback {
+    rq_matvec_fn fn;
+    void *ctx;
+    int operator()(int32_t vt, const void *in, void *out, cudaStream_t s, State *,
+                   bool refresh) const {
+        if (refresh) return RQ_OK;  // callbacks run the REFERENCE variant
+        const int rc = fn(ctx, vt, in, out, s);
+        return rc == 0 ? RQ_OK : fail(RQ_E_ARG, "rq_lobpcg_solve_cb: the matvec callback failed");
+    }
+};
+
+template <typename V, typename SEG, typename MV>
+struct Phase {
+    MV mv;
     int32_t vtype;
-    State *st;
-    void *red;
-    void *mvscratch;  // scratch for the matvec (its error flag)
-    Vecs<V> v;
-    int64_t D;
+    SEG seg;
     int grid;
+    State *states;
+    int P;
+    int *nactive;
+    Vecs<V> v;
     bool jacobi;
     const double *diag;
 
-    int matvec(const V *in, V *out, cudaStream_t s, const int *gate2 = nullptr) {
-        ++issued;
-        if (fn) {
-            if (gate2) return RQ_OK;  // FAST refreshes need the gate; callbacks use REFERENCE
-            const int rc = fn(ctx, vtype, in, out, s);
-            return rc == 0 ? RQ_OK : fail(RQ_E_ARG, "rq_lobpcg_solve_cb: the matvec callback failed");
-        }
-        return matvec_dispatch(*op, vtype, in, out, mvscratch, s, &st->active, gate2);
+    int pgrid() const { return (P + 127) / 128; }
+
+    int matvec(const V *in, V *out, cudaStream_t s, bool refresh = false) {
+        return mv(vtype, in, out, s, states, refresh);
     }
-    int issued = 0;
 
     // project_out((x, y), src) -> p  (ground_locg.py:380-421); src is overwritten
     void project(V *src, cudaStream_t s) {
         Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
-        k_dots<V, 2><<<grid, kThreads, 0, s>>>(st, D, pr, kIp0, red);
-        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
-        k_scale_dots2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, 1, red);
-        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
-        k_scale_dots2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, 1, red);
-        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
-        k_scale_dots2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, 0, red);
-        k_sub2_norm<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, src, red);
-        k_mask<V><<<grid, kThreads, 0, s>>>(st, D, src, v.p);
+        k_dots<V, 2, SEG><<<grid, kThreads, 0, s>>>(seg, pr, kIp0);
+        k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
+        k_scale_dots2<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src, 1);
+        k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
+        k_scale_dots2<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src, 1);
+        k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
+        k_scale_dots2<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src, 0);
+        k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
+        k_mask<V, SEG><<<grid, kThreads, 0, s>>>(seg, src, v.p);
     }
 
     // one loop iteration (ground_locg.py:288-341)
     int iteration(int variant, cudaStream_t s) {
         V *src = v.r;
         if (jacobi) {
-            k_jacobi<V><<<grid, kThreads, 0, s>>>(st, D, diag, v.r, v.w);
+            k_jacobi<V, SEG><<<grid, kThreads, 0, s>>>(seg, diag, v.r, v.w);
             src = v.w;
         }
         project(src, s);
@@ -699,22 +827,23 @@ struct Phase {
             RQ_TRY(matvec(v.y, v.ay, s));
         }
         RQ_TRY(matvec(v.p, v.ap, s));
-        k_gram3<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, v.ax, v.ay, v.ap, red);
-        k_rr3<<<1, 1, 0, s>>>(st);
-        k_upd_s<V><<<grid, kThreads, 0, s>>>(st, D, v.y, v.p, red);
-        k_upd_tu<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, red);
+        k_gram3<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+        k_rr3<<<pgrid(), 128, 0, s>>>(states, P);
+        k_upd_s<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.y, v.p);
+        k_upd_tu<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p);
         if (variant == RQ_LOBPCG_REFERENCE) {
-            k_upd_xy<V, false><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, nullptr, nullptr, nullptr);
+            k_upd_xy<V, false, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p, nullptr, nullptr,
+                                                              nullptr);
             RQ_TRY(matvec(v.x, v.ax, s));
         } else {
-            k_upd_xy<V, true><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+            k_upd_xy<V, true, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
             // periodic / certifying refresh of the carried products
-            RQ_TRY(matvec(v.x, v.ax, s, &st->want_refresh));
-            RQ_TRY(matvec(v.y, v.ay, s, &st->want_refresh));
-            k_refresh_mark<<<1, 1, 0, s>>>(st);
+            RQ_TRY(matvec(v.x, v.ax, s, true));
+            RQ_TRY(matvec(v.y, v.ay, s, true));
+            k_refresh_mark<<<pgrid(), 128, 0, s>>>(states, P);
         }
-        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
-        k_check<<<1, 1, 0, s>>>(st);
+        k_resid<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.ax, v.x, v.r, 0);
+        k_check<<<pgrid(), 128, 0, s>>>(states, P, nactive);
         RQ_CUDA(cudaGetLastError());
         return RQ_OK;
     }
@@ -723,23 +852,23 @@ struct Phase {
     // A y for its carried products
     int start(int variant, cudaStream_t s) {
         Pairs<V, 1> nx{{v.x}, {v.x}};
-        k_dots<V, 1><<<grid, kThreads, 0, s>>>(st, D, nx, kMisc2, red);
-        k_normalize<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.x, kMisc2);
+        k_dots<V, 1, SEG><<<grid, kThreads, 0, s>>>(seg, nx, kMisc2);
+        k_normalize<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.x, kMisc2);
         RQ_TRY(matvec(v.x, v.ax, s));
         Pairs<V, 1> rho{{v.x}, {v.ax}};
-        k_dots<V, 1><<<grid, kThreads, 0, s>>>(st, D, rho, kMisc, red);
-        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 1, red);
+        k_dots<V, 1, SEG><<<grid, kThreads, 0, s>>>(seg, rho, kMisc);
+        k_resid<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.ax, v.x, v.r, 1);
         // iteration 1: p = r / |r|
-        k_normalize<V><<<grid, kThreads, 0, s>>>(st, D, v.r, v.p, kRn);
+        k_normalize<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.r, v.p, kRn);
         RQ_TRY(matvec(v.x, v.ax, s));
         RQ_TRY(matvec(v.p, v.ap, s));
-        k_gram2<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.p, v.ax, v.ap, red);
-        k_rr2<<<1, 1, 0, s>>>(st);
-        k_upd2_norms<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.p, red);
-        k_upd2_xy<V><<<grid, kThreads, 0, s>>>(st, D, v.x, v.y, v.p);
+        k_gram2<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.p, v.ax, v.ap);
+        k_rr2<<<pgrid(), 128, 0, s>>>(states, P);
+        k_upd2_norms<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.p);
+        k_upd2_xy<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p);
         RQ_TRY(matvec(v.x, v.ax, s));
         if (variant == RQ_LOBPCG_FAST) RQ_TRY(matvec(v.y, v.ay, s));
-        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
+        k_resid<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.ax, v.x, v.r, 0);
         RQ_CUDA(cudaGetLastError());
         return RQ_OK;
     }
@@ -748,44 +877,23 @@ struct Phase {
     int resume(int variant, cudaStream_t s) {
         RQ_TRY(matvec(v.x, v.ax, s));
         if (variant == RQ_LOBPCG_FAST) RQ_TRY(matvec(v.y, v.ay, s));
-        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
-        RQ_CUDA(cudaGetLastError());
-        return RQ_OK;
-    }
-
-    // FAST: A x and A y recomputed (gated by want_refresh through a copy of the flag)
-    int refresh(cudaStream_t s) {
-        RQ_TRY(matvec(v.x, v.ax, s));
-        RQ_TRY(matvec(v.y, v.ay, s));
-        k_resid<V><<<grid, kThreads, 0, s>>>(st, D, v.ax, v.x, v.r, 0, red);
+        k_resid<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.ax, v.x, v.r, 0);
         RQ_CUDA(cudaGetLastError());
         return RQ_OK;
     }
 };
 
-struct HostState {
-    int iter, active, converged, status;
-};
-
-int read_flags(State *st, HostState &h, cudaStream_t s) {
-    int buf[4];
-    RQ_CUDA(cudaMemcpyAsync(buf, &st->iter, sizeof(int), cudaMemcpyDeviceToHost, s));
-    RQ_CUDA(cudaMemcpyAsync(buf + 1, &st->active, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    RQ_CUDA(cudaMemcpyAsync(buf + 3, &st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+int read_active(const int *nactive, int &h, cudaStream_t s) {
+    RQ_CUDA(cudaMemcpyAsync(&h, nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
     RQ_CUDA(cudaStreamSynchronize(s));
-    h.iter = buf[0];
-    h.active = buf[1];
-    h.converged = buf[2];
-    h.status = buf[3];
     return RQ_OK;
 }
 
-// Run iterations until the state goes inactive.  With use_graph the chunk is captured once and
-// relaunched; otherwise launched eagerly.
-template <typename V>
-int run_loop(Phase<V> &ph, int variant, bool use_graph, cudaStream_t s) {
-    HostState h{};
-    const int chunk = ph.fn ? 1 : kChunk;
+// Run iterations until no problem is active.  With use_graph the chunk is captured once and
+// relaunched; otherwise launched eagerly.  Callbacks run one iteration per chunk.
+template <typename PH>
+int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s) {
+    int active = 0;
     auto enqueue_chunk = [&](cudaStream_t cs) -> int {
         for (int k = 0; k < chunk; ++k) RQ_TRY(ph.iteration(variant, cs));
         return RQ_OK;
@@ -793,8 +901,8 @@ int run_loop(Phase<V> &ph, int variant, bool use_graph, cudaStream_t s) {
     if (!use_graph) {
         while (true) {
             RQ_TRY(enqueue_chunk(s));
-            RQ_TRY(read_flags(ph.st, h, s));
-            if (!h.active) break;
+            RQ_TRY(read_active(ph.nactive, active, s));
+            if (active <= 0) break;
         }
         return RQ_OK;
     }
@@ -814,84 +922,120 @@ int run_loop(Phase<V> &ph, int variant, bool use_graph, cudaStream_t s) {
     while (true) {
         e = cudaGraphLaunch(exec, s);
         if (e != cudaSuccess) break;
-        rc = read_flags(ph.st, h, s);
-        if (rc != RQ_OK || !h.active) break;
+        rc = read_active(ph.nactive, active, s);
+        if (rc != RQ_OK || active <= 0) break;
     }
     cudaGraphExecDestroy(exec);
     RQ_CUDA(e);
     return rc;
 }
 
-template <typename V>
-int init_state(State *st, const rq_lobpcg_params_t &p, double tol, double tol_dim, bool lo,
-               int maxiter, cudaStream_t s) {
-    State h{};
-    h.tol = tol;
-    h.tol_dim = tol_dim;
-    h.switch_rel = p.switch_rel > 0 ? p.switch_rel : 1e-5;
-    h.target_rel = lo ? 0. : p.target_rel;
-    h.best_r = INFINITY;
-    h.maxiter = maxiter;
-    h.active = 1;
-    h.phase_lo = lo ? 1 : 0;
-    h.refresh = p.refresh > 0 ? p.refresh : 32;
-    h.variant = p.variant;
-    h.guard = p.guard;
-    RQ_CUDA(cudaMemcpyAsync(st, &h, sizeof(State), cudaMemcpyHostToDevice, s));
-    RQ_CUDA(cudaStreamSynchronize(s));  // h is a stack object
+// Per-problem state initialisation (tol_dim per problem), and the count of active problems.
+int init_states(State *dev, int *nactive, int P, const rq_lobpcg_params_t &p, double tol,
+                const std::vector<double> &tol_dim, bool lo, cudaStream_t s) {
+    std::vector<State> h(P);
+    for (int q = 0; q < P; ++q) {
+        State &st = h[q];
+        std::memset(&st, 0, sizeof(State));
+        st.tol = tol;
+        st.tol_dim = tol_dim[q];
+        st.switch_rel = p.switch_rel > 0 ? p.switch_rel : 1e-5;
+        st.target_rel = lo ? 0. : p.target_rel;
+        st.best_r = INFINITY;
+        st.maxiter = p.maxiter;
+        st.active = 1;
+        st.phase_lo = lo ? 1 : 0;
+        st.refresh = p.refresh > 0 ? p.refresh : 32;
+        st.variant = p.variant;
+        st.guard = p.guard;
+    }
+    RQ_CUDA(cudaMemcpyAsync(dev, h.data(), sizeof(State) * P, cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(nactive, &P, sizeof(int), cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaStreamSynchronize(s));  // host sources are stack objects
     return RQ_OK;
 }
 
-template <typename VLO, typename VHI>
-int solve(const rq_operator_t &op, rq_matvec_fn fn, void *ctx, const rq_lobpcg_params_t &p,
-          char *ws, const void *x0, void *xout, rq_lobpcg_result_t *res, cudaStream_t s) {
+double eps_of(int32_t vt) {
+    return (vt == RQ_F32 || vt == RQ_C64) ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+}
+
+void fill_result(const State &h, int niter_lo, const rq_lobpcg_params_t &p, rq_lobpcg_result_t *res) {
+    res->eigval = p.maxiter > 0 ? h.theta : 0.;  // the loop's initial theta (ground_locg.py:358)
+    res->resnorm = h.resnorm;
+    res->axnorm = h.axnorm;
+    res->niter = h.iter + niter_lo;
+    res->niter_lo = niter_lo;
+    res->matvecs = 0;
+    res->converged = h.converged;
+    res->status = h.status ? h.status : (h.converged ? RQ_OK : RQ_E_MAXITER);
+}
+
+// Two-phase driver shared by the single-problem and the batched solves: an optional 32-bit phase,
+// then the final value type.  `mk_lo` / `mk_hi` build the phases over their vectors.
+template <typename PLO, typename PHI>
+int run_phases(PLO &lo, PHI &hi, bool mixed, const rq_lobpcg_params_t &p, double tol,
+               const std::vector<double> &tol_dim, int64_t D, const void *x0, size_t hi_bytes,
+               int chunk, bool graph, cudaStream_t s, std::vector<int> &niter_lo) {
+    using VLO = typename std::remove_pointer<decltype(lo.v.x)>::type;
+    using VHI = typename std::remove_pointer<decltype(hi.v.x)>::type;
+    const int P = hi.P;
+    niter_lo.assign(P, 0);
+    const int gconv = (int)std::min<int64_t>((D + kThreads - 1) / kThreads, (int64_t)sm_count() * 8);
+    if (mixed) {
+        RQ_TRY(init_states(lo.states, lo.nactive, P, p, eps_of(lo.vtype), tol_dim, true, s));
+        k_convert<VHI, VLO><<<gconv, kThreads, 0, s>>>(D, static_cast<const VHI *>(x0), lo.v.x);
+        RQ_TRY(lo.start(p.variant, s));
+        if (p.maxiter > 0) RQ_TRY(run_loop(lo, p.variant, graph, chunk, s));
+        std::vector<State> h(P);
+        RQ_CUDA(cudaMemcpyAsync(h.data(), lo.states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
+        RQ_CUDA(cudaStreamSynchronize(s));
+        for (int q = 0; q < P; ++q) niter_lo[q] = h[q].iter;
+        // continue in the final type from x and y, each problem with its own theta
+        k_convert<VLO, VHI><<<gconv, kThreads, 0, s>>>(D, lo.v.x, hi.v.x);
+        k_convert<VLO, VHI><<<gconv, kThreads, 0, s>>>(D, lo.v.y, hi.v.y);
+        RQ_TRY(init_states(hi.states, hi.nactive, P, p, tol, tol_dim, false, s));
+        std::vector<State> h2(P);
+        RQ_CUDA(cudaMemcpyAsync(h2.data(), hi.states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
+        RQ_CUDA(cudaStreamSynchronize(s));
+        for (int q = 0; q < P; ++q) h2[q].theta = h[q].theta;
+        RQ_CUDA(cudaMemcpyAsync(hi.states, h2.data(), sizeof(State) * P, cudaMemcpyHostToDevice, s));
+        RQ_TRY(hi.resume(p.variant, s));
+        RQ_CUDA(cudaStreamSynchronize(s));  // h2 is a stack vector
+    } else {
+        RQ_TRY(init_states(hi.states, hi.nactive, P, p, tol, tol_dim, false, s));
+        RQ_CUDA(cudaMemcpyAsync(hi.v.x, x0, hi_bytes, cudaMemcpyDeviceToDevice, s));
+        RQ_TRY(hi.start(p.variant, s));
+    }
+    if (p.maxiter > 0) RQ_TRY(run_loop(hi, p.variant, graph, chunk, s));
+    return RQ_OK;
+}
+
+template <typename VLO, typename VHI, typename MV>
+int solve(const rq_operator_t &op, MV mv, bool callback, const rq_lobpcg_params_t &p, char *ws,
+          const void *x0, void *xout, rq_lobpcg_result_t *res, cudaStream_t s) {
     const int64_t D = op.sub.D;
     const Layout L = layout(D, p);
     State *st = reinterpret_cast<State *>(ws + L.state);
+    int *nactive = reinterpret_cast<int *>(ws + L.err + 8);
     void *red = ws + L.red;
-    // the matvec's scratch: its error flag sits 16 bytes into the area we hand it
-    void *mvscratch = ws + L.err - kScratchErr;
     RQ_CUDA(cudaMemsetAsync(ws + L.err, 0, 16, s));
     RQ_CUDA(cudaMemsetAsync(red, 0, 16, s));
-    const double tol_dim = p.tol_dim > 0 ? p.tol_dim : (double)D;
+    const std::vector<double> tol_dim(1, p.tol_dim > 0 ? p.tol_dim : (double)D);
     const bool jac = p.jacobi != 0 && op.diag0 != nullptr;
     const int grid = grid_vec(D);
-    const int hi_type = p.vtype;
-    const bool cplx = (hi_type == RQ_C64 || hi_type == RQ_C128);
-    const double eps_hi = (hi_type == RQ_F32 || hi_type == RQ_C64) ? 1.1920928955078125e-07
-                                                                   : 2.220446049250313e-16;
-    const double tol = p.tol > 0 ? p.tol : eps_hi;
-    (void)cplx;
-
-    Phase<VHI> hi{fn, ctx, &op, hi_type, st, red, mvscratch,
-                  carve_vecs<VHI>(ws + L.vec_hi, L.hi_bytes), D, grid, jac, op.diag0};
-    int niter_lo = 0, matvec_lo = 0;
-    if (p.mixed && lo_type(hi_type) != hi_type) {
-        Phase<VLO> lo{fn, ctx, &op, lo_type(hi_type), st, red, mvscratch,
-                      carve_vecs<VLO>(ws + L.vec_lo, L.lo_bytes), D, grid, jac, op.diag0};
-        RQ_TRY(init_state<VLO>(st, p, 1.1920928955078125e-07, tol_dim, true, p.maxiter, s));
-        k_convert<VHI, VLO><<<grid, kThreads, 0, s>>>(D, static_cast<const VHI *>(x0), lo.v.x);
-        RQ_TRY(lo.start(p.variant, s));
-        if (p.maxiter > 0) RQ_TRY(run_loop<VLO>(lo, p.variant, p.use_graph != 0, s));
-        HostState h{};
-        RQ_TRY(read_flags(st, h, s));
-        niter_lo = h.iter;
-        // continue in the 64-bit type from x and y
-        k_convert<VLO, VHI><<<grid, kThreads, 0, s>>>(D, lo.v.x, hi.v.x);
-        k_convert<VLO, VHI><<<grid, kThreads, 0, s>>>(D, lo.v.y, hi.v.y);
-        double theta_lo = 0.;
-        RQ_CUDA(cudaMemcpyAsync(&theta_lo, &st->theta, sizeof(double), cudaMemcpyDeviceToHost, s));
-        RQ_CUDA(cudaStreamSynchronize(s));
-        RQ_TRY(init_state<VHI>(st, p, tol, tol_dim, false, p.maxiter, s));
-        RQ_CUDA(cudaMemcpyAsync(&st->theta, &theta_lo, sizeof(double), cudaMemcpyHostToDevice, s));
-        RQ_TRY(hi.resume(p.variant, s));
-        RQ_CUDA(cudaStreamSynchronize(s));  // theta_lo is a stack value
-    } else {
-        RQ_TRY(init_state<VHI>(st, p, tol, tol_dim, false, p.maxiter, s));
-        RQ_CUDA(cudaMemcpyAsync(hi.v.x, x0, L.hi_bytes, cudaMemcpyDeviceToDevice, s));
-        RQ_TRY(hi.start(p.variant, s));
-    }
-    if (p.maxiter > 0) RQ_TRY(run_loop<VHI>(hi, p.variant, p.use_graph != 0, s));
+    const int32_t hi_type = p.vtype;
+    const double tol = p.tol > 0 ? p.tol : eps_of(hi_type);
+    const bool mixed = p.mixed && lo_type(hi_type) != hi_type;
+    SegOne seg{st, D, red};
+    Phase<VHI, SegOne, MV> hi{mv, hi_type, seg, grid, st, 1, nactive,
+                              carve_vecs<VHI>(ws + L.vec_hi, L.hi_bytes), jac, op.diag0};
+    Phase<VLO, SegOne, MV> lo{mv, lo_type(hi_type), seg, grid, st, 1, nactive,
+                              carve_vecs<VLO>(ws + (mixed ? L.vec_lo : L.vec_hi), L.lo_bytes),
+                              jac, op.diag0};
+    std::vector<int> nlo;
+    const bool graph = p.use_graph != 0 && !callback;
+    RQ_TRY(run_phases(lo, hi, mixed, p, tol, tol_dim, D, x0, L.hi_bytes, callback ? 1 : kChunk,
+                      graph, s, nlo));
     State h{};
     int mv_err = 0;
     RQ_CUDA(cudaMemcpyAsync(&h, st, sizeof(State), cudaMemcpyDeviceToHost, s));
@@ -899,15 +1043,7 @@ int solve(const rq_operator_t &op, rq_matvec_fn fn, void *ctx, const rq_lobpcg_p
     RQ_CUDA(cudaMemcpyAsync(xout, hi.v.x, L.hi_bytes, cudaMemcpyDeviceToDevice, s));
     RQ_CUDA(cudaStreamSynchronize(s));
     if (mv_err) return fail(mv_err, "rq_lobpcg_solve: matvec reported an error");
-    res->eigval = p.maxiter > 0 ? h.theta : 0.;  // the loop's initial theta (ground_locg.py:358)
-    res->resnorm = h.resnorm;
-    res->axnorm = h.axnorm;
-    res->niter = h.iter + niter_lo;
-    res->niter_lo = niter_lo;
-    (void)matvec_lo;
-    res->matvecs = 0;
-    res->converged = h.converged;
-    res->status = h.status ? h.status : (h.converged ? RQ_OK : RQ_E_MAXITER);
+    fill_result(h, nlo[0], p, res);
     return RQ_OK;
 }
 
@@ -966,13 +1102,19 @@ int solve_entry(const rq_operator_t *op, rq_matvec_fn fn, void *ctx, const rq_lo
     }
     char *ws = static_cast<char *>(workspace);
     int rc;
+    const Layout L = layout(op->sub.D, *prm);
+    void *mvscratch = ws + L.err - kScratchErr;  // the matvec's error flag at ws + L.err
+#define RQ_SOLVE(VLO, VHI)                                                                   \
+    (fn ? solve<VLO, VHI>(*op, MvCallback{fn, ctx}, true, *prm, ws, x0, x_out, res, s)       \
+        : solve<VLO, VHI>(*op, MvOne{op, mvscratch}, false, *prm, ws, x0, x_out, res, s))
     switch (vt) {
-        case RQ_F32: rc = solve<float, float>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
-        case RQ_F64: rc = solve<float, double>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
-        case RQ_C64: rc = solve<float2, float2>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
-        case RQ_C128: rc = solve<float2, double2>(*op, fn, ctx, *prm, ws, x0, x_out, res, s); break;
+        case RQ_F32: rc = RQ_SOLVE(float, float); break;
+        case RQ_F64: rc = RQ_SOLVE(float, double); break;
+        case RQ_C64: rc = RQ_SOLVE(float2, float2); break;
+        case RQ_C128: rc = RQ_SOLVE(float2, double2); break;
         default: rc = fail(RQ_E_ARG, "rq_lobpcg_solve: bad vtype");
     }
+#undef RQ_SOLVE
     if (priv) {
         cudaStreamSynchronize(priv);
         cudaStreamDestroy(priv);
