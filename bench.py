@@ -368,6 +368,154 @@ def run_ours(args, rank, ws):
         print(json.dumps(line), flush=True)
 
 
+class BatchWorkload:
+    """256 independent random Pauli-sum problems (N uniform in 16..40, K log-uniform in
+    100..2000, D log-uniform in 2^10..2^18 capped at half the weight-N/2 sector), seed 2."""
+
+    def __init__(self, P=256, seed=2):
+        from rqutils_gb300 import workloads as W
+        from rqutils_gb300.paulis.symplectic import PauliSumXZ
+        self.name = 'batched'
+        self.seed = seed
+        raw, self.S, self.ns = W.batched_random_problems(seed, P=P)
+        self.raw = raw
+        self.hams = [PauliSumXZ.from_paulisum(h, force_real=True, add_padding=True) for h in raw]
+        self.P = P
+        self.D = int(sum(len(s) for s in self.S))
+        self.x = W.random_vector(np.random.default_rng(seed + 1), self.D, complex_=True)
+        self.vtype = 'c64'
+        self.label = f'batched{P}_random_N16to40_K100to2000_D2e10to2e18_weightN2'
+
+    def config(self, extra=None):
+        cfg = {'workload': self.label, 'problems': self.P, 'D_total': self.D,
+               'groups_total': int(sum(len(h.xmask) for h in self.hams)),
+               'terms_total': int(sum(len(h.zmask) for h in self.hams)),
+               'vector_type': self.vtype,
+               'matvec_mode': 'matrix-free batched (one hash table over (problem, state) keys)',
+               'l2_policy': 'flush 256 MiB between timed steps', 'seed': self.seed,
+               'value_counts': 'problem matvecs (one batched launch = P of them)'}
+        if extra:
+            cfg.update(extra)
+        return cfg
+
+
+def run_batched(args, rank, ws):
+    import torch
+    from rqutils_gb300.batch import BatchedSQD
+    from rqutils_gb300.ground_locg import lobpcg_solve
+    from rqutils_gb300.sqd import SQDProblem
+
+    dev = torch.device('cuda', torch.cuda.current_device())
+    wl = BatchWorkload()
+    t0 = time.perf_counter()
+    b_free = BatchedSQD(wl.hams, wl.S, cache_level=(0, 0), device=dev)
+    t_build = time.perf_counter() - t0
+    b_conn = BatchedSQD(wl.hams, wl.S, cache_level=(1, 0), device=dev)
+    hits = b_conn.nnz
+    x = torch.as_tensor(wl.x).to(dev, torch.complex64)
+    y = torch.empty_like(x)
+    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def flush():
+        flush_buf.fill_(1.0)
+
+    clk = ClockSampler(index=torch.cuda.current_device()).__enter__()
+    for _ in range(args.warmup):
+        b_free.matvec(x, out=y)
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    times = time_steps(lambda: b_free.matvec(x, out=y), args.steps, flush, stream)
+    wall = time.perf_counter() - t0
+    barrier(ws)
+    b_free.check_errors()
+    t_step = max_over_ranks(sum(times) / 1e3, ws)
+    ms_per_step = 1e3 * t_step / args.steps
+    value = ws * wl.P * args.steps / t_step
+    y_conn = b_conn.matvec(x)
+    rel = float(torch.linalg.vector_norm(y - y_conn) / torch.linalg.vector_norm(y_conn))
+    for _ in range(args.warmup):
+        b_conn.matvec(x, out=y)
+    t_conn = statistics.mean(time_steps(lambda: b_conn.matvec(x, out=y), max(3, args.steps),
+                                        flush, stream))
+
+    xh = torch.as_tensor(wl.x.astype(np.complex64)).pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    xd = torch.empty_like(x)
+
+    def e2e_step():
+        xd.copy_(xh, non_blocking=True)
+        b_free.matvec(xd, out=y)
+        yh.copy_(y, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    e2e_t = max_over_ranks(sum(time_steps(e2e_step, args.steps, flush, stream)) / 1e3, ws)
+    clk.__exit__(None, None, None)
+
+    # roofline: every problem's algorithmic bytes summed
+    bv = 8
+    abytes = 8 * wl.D + 2 * bv * wl.D + bv * hits
+    for h, S in zip(wl.hams, wl.S):
+        J0 = 1 if np.any(h.xmask == 0) else 0
+        abytes += 8 * len(S) * (len(h.xmask) - J0)
+    peak, peak_kind = measured_peaks()
+    achieved = abytes / (ms_per_step / 1e3) / 1e9
+
+    # batched LOBPCG of all problems (cached connectivity, mixed precision, relative residual
+    # 1e-8, seeded random start) against the same solver run problem by problem on a sample
+    rng = np.random.default_rng(wl.seed + 2)
+    xr = rng.normal(size=wl.D) + 1j * rng.normal(size=wl.D)
+    x0 = torch.as_tensor(xr.real if b_conn.is_real else xr).to(dev, b_conn.dtype)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eig, xs, infos = b_conn.solve(x0=x0, precision='mixed', variant='fast', target_rel=1e-8,
+                                  maxiter=5000)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    its = [i['niter'] for i in infos]
+    nsample = 16
+    t_single = 0.
+    for p in range(nsample):
+        prob = SQDProblem(wl.hams[p], wl.S[p], cache_level=(1, 0), device=dev)
+        xp = x0[b_conn.rows(p)].contiguous()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lobpcg_solve(prob.op, xp, maxiter=5000, target_rel=1e-8, mixed=True, variant='fast')
+        torch.cuda.synchronize()
+        t_single += time.perf_counter() - t0
+    lob = {'batched_mixed_fast': {
+        'start': 'random (seeded)', 'time_s': round(t_batch, 4),
+        'iterations_max': int(max(its)), 'iterations_median': float(np.median(its)),
+        'converged': int(sum(i['converged'] for i in infos)), 'problems': wl.P},
+        'one_by_one_mixed_fast_estimate_s': round(t_single * wl.P / nsample, 3),
+        'one_by_one_sample': f'first {nsample} problems solved alone, scaled to {wl.P}'}
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': wl.vtype, 'data': 'synthetic',
+        'config': wl.config({'parallelism': f'replicas{ws}' if ws > 1 else 'single',
+                             'hits_per_matvec': hits, 'build_s': round(t_build, 3),
+                             'wall_s_timed_region': round(wall, 3)}),
+        'e2e': {'value': ws * wl.P * args.steps / e2e_t, 'unit': UNIT,
+                'h2d_bytes_per_step': bv * wl.D, 'd2h_bytes_per_step': bv * wl.D},
+        'gpu_launches': args.steps,
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': None,
+                     'peak_source': f'{peak_kind} hbm_gbs',
+                     'algorithmic_bytes_per_launch': abytes},
+        'modes': {'conn_problem_matvec_per_s': wl.P * 1e3 / t_conn,
+                  'free_vs_conn_rel_diff': rel},
+        'lobpcg': lob,
+        'clocks': clk.summary(),
+    }
+    if rank == 0:
+        line['cpu_baseline'] = cpu_baseline_batched(wl, budget_s=12.0)
+        print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     """Only the timed loop of the headline (warm-up, then flush + matvec per step): the command
     that the ncu launch list and the kernel capture are taken on."""
@@ -458,8 +606,46 @@ def cpu_baseline(wl, budget_s=12.0, steps=None):
     return {'value': 1.0 / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port', 'sample': sample}
 
 
+def cpu_baseline_batched(wl, budget_s=12.0):
+    """The oracle's apply_h restatement problem by problem (complex128, groups over all cores),
+    on as many problems as fit the budget, scaled to the batch by rows x groups."""
+    from oracle.sqd import matvec_nocache
+    cores = os.cpu_count() or 1
+    work = np.array([len(S) * len(h.xmask) for h, S in zip(wl.hams, wl.S)], dtype=np.float64)
+    done, spent, p = 0., 0., 0
+    while p < wl.P and spent < budget_s:
+        terms = _oracle_setup(wl.hams[p])
+        rows = slice(int(sum(len(s) for s in wl.S[:p])), int(sum(len(s) for s in wl.S[:p + 1])))
+        xp = wl.x[rows].astype(np.complex128)
+        t0 = time.perf_counter()
+        matvec_nocache(xp, terms, wl.S[p], threads=cores)
+        spent += time.perf_counter() - t0
+        done += work[p]
+        p += 1
+    dt = spent * work.sum() / done  # seconds for one matvec of every problem
+    return {'value': wl.P / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': f'one matvec of each of the first {p} of {wl.P} problems ({spent:.1f} s), '
+                      'scaled to the batch by rows x groups; complex128, NumPy restatement of '
+                      'apply_h with per-group sort-merge'}
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
+        return
+    if args.workload == 'batched':
+        wl = BatchWorkload()
+        cb = cpu_baseline_batched(wl, budget_s=min(60.0, 6.0 * max(1, args.steps)))
+        v = cb['value']
+        print(json.dumps({
+            'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': ws,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * wl.P / v,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128',
+            'data': 'synthetic',
+            'config': wl.config({'note': 'the reference JAX path cannot be installed here (no '
+                                         'jax); the NumPy restatement of its algorithm is timed'}),
+            'cpu_baseline': cb,
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        }), flush=True)
         return
     wl = Workload(args.workload, args.rows)
     # bounded sample sized so that the whole run stays within a few minutes
@@ -487,9 +673,11 @@ def main():
                     help='run only the timed matvec loop (for ncu captures)')
     ap.add_argument('--rows', type=int, default=None,
                     help='override the subspace dimension (profiling captures on a small case)')
-    ap.add_argument('--workload', default='hubbard', choices=['hubbard', 'chemistry', 'random20'],
+    ap.add_argument('--workload', default='hubbard',
+                    choices=['hubbard', 'chemistry', 'random20', 'batched'],
                     help='hubbard: Hubbard 4x4, D=2^20 (the headline); chemistry: 64 qubits, '
-                         '50,000 terms, D=2^26; random20: 20 qubits, 200 terms, D=16384')
+                         '50,000 terms, D=2^26; random20: 20 qubits, 200 terms, D=16384; '
+                         'batched: 256 random problems of 16..40 qubits in one launch')
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == 'ours':
         args.warmup = 3
@@ -503,7 +691,10 @@ def main():
         run_profile(args)
         return
     rank, ws = dist_init()
-    run_ours(args, rank, ws)
+    if args.workload == 'batched':
+        run_batched(args, rank, ws)
+    else:
+        run_ours(args, rank, ws)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

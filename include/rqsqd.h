@@ -12,6 +12,8 @@
  *   rq_lobpcg_solve        ground_locg / _ground_locg_callable            rqutils/ground_locg.py:128-377
  *   rq_lobpcg_solve_cb     ground_locg with a user matvec or matrix      rqutils/ground_locg.py:154-179
  *   rq_eigenpair_3x3       eigenpair_3x3                                 rqutils/ground_locg.py:438-471
+ *   rq_batch_*             sqd() over many problems (no batched form in the reference; each
+ *                          problem is the reference's sqd.py:299-411 / ground_locg.py:182-377)
  *
  * Conventions
  *   - A basis state is a uint64 whose bit q is qubit q.  Subspaces are strictly increasing arrays
@@ -219,6 +221,56 @@ int rq_lobpcg_solve_cb(int64_t D, rq_matvec_fn fn, void *ctx, const rq_lobpcg_pa
 /* Lowest eigenpair of a Hermitian 3x3 (row-major complex double [18]) on the device, Cardano as
  * ground_locg.py:438-471: writes lambda to out[0] and the eigenvector (complex) to out[2..7]. */
 int rq_eigenpair_3x3(const double *mat, double *out, void *stream);
+
+/* ---- batches of independent problems ------------------------------------------------------ */
+
+#define RQ_BATCH_STATE_BITS 40   /* composite key = (problem << 40) | state; states < 2^40 */
+
+typedef struct rq_batch {
+    int32_t  P;                /* number of problems (< 2^24)                                   */
+    int32_t  mode;             /* RQ_MODE_FREE or RQ_MODE_CONN                                   */
+    const uint64_t *keys;      /* [D] composite keys, strictly increasing (problems in order)   */
+    const int64_t  *prow;      /* [P + 1] first row of each problem                              */
+    int64_t  D;                /* total rows                                                     */
+    void    *hkeys;            /* hash table over the composite keys: 32 << hbits bytes          */
+    int32_t *hvals;            /* [4 << hbits]                                                   */
+    int32_t  hbits;            /* rq_subspace_sizes(D, 64, &hbits)                               */
+    int32_t  pad_;
+    uint64_t empty_key;        /* written by rq_batch_build                                      */
+    const uint64_t *fmask;     /* [2P] sector filter masks (a, b) of each problem; NULL = off    */
+    uint32_t *fbits;           /* [P * RQ_FILTER_WORDS], written by rq_batch_build               */
+    rq_terms_t terms;          /* every problem's X groups concatenated (toff over all terms)   */
+    const int32_t *gofs;       /* [P + 1] first group of each problem                            */
+    const int32_t *dgrp;       /* [P] global index of each problem's x = 0 group, or -1          */
+    double  *diag0;            /* [D] x = 0 diagonal of each row, written by rq_batch_build      */
+    const int64_t *rowptr;     /* [D + 1]  RQ_MODE_CONN                                          */
+    const int32_t *col;        /* [nnz]    source row (global index)                             */
+    const int32_t *grp;        /* [nnz]    X group (global index)                                */
+    int64_t  nnz;
+    const int64_t *states_size; /* [P] HOST array: each problem's convergence length (sqd's
+                                   states_size, sqd.py:222-225); NULL = its row count        */
+} rq_batch_t;
+
+/* Validate the keys, fill the hash table, the per-problem sector filters and diag0.
+ * Synchronises the stream.  Many independent Pauli sums on their own subspaces are solved
+ * together: one launch per step serves all problems.  Every X mask must fit in the state bits
+ * (below bit RQ_BATCH_STATE_BITS); rq_batch_build rejects one that does not. */
+int rq_batch_build(rq_batch_t *b, void *scratch, void *stream);
+
+/* Connectivity of every row (RQ_MODE_CONN), two passes as rq_conn_build. */
+int rq_batch_conn_build(const rq_batch_t *b, int64_t *rowptr, int32_t *col, int32_t *grp,
+                        int64_t *nnz, void *scratch, void *stream);
+
+/* y = H_p x on every problem's rows at once. */
+int rq_batch_matvec(const rq_batch_t *b, int32_t vtype, const void *x, void *y, void *scratch,
+                    void *stream);
+
+/* LOBPCG on all problems together (rows of every problem in one vector, per-problem reductions,
+ * Rayleigh-Ritz and convergence; converged problems stop).  res has P entries; the convergence
+ * test of problem p uses states_size[p] (or its row count). */
+int rq_batch_workspace_size(const rq_batch_t *b, const rq_lobpcg_params_t *prm, size_t *bytes);
+int rq_batch_solve(const rq_batch_t *b, const rq_lobpcg_params_t *prm, void *workspace,
+                   const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
 
 /* ---- diagnostics ------------------------------------------------------------------------- */
 

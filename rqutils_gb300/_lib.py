@@ -59,6 +59,18 @@ class LobpcgResult(ctypes.Structure):
                 ('pad_', ctypes.c_int32)]
 
 
+class Batch(ctypes.Structure):
+    _fields_ = [('P', ctypes.c_int32), ('mode', ctypes.c_int32), ('keys', _c_void_p),
+                ('prow', _c_void_p), ('D', ctypes.c_int64), ('hkeys', _c_void_p),
+                ('hvals', _c_void_p), ('hbits', ctypes.c_int32), ('pad_', ctypes.c_int32),
+                ('empty_key', ctypes.c_uint64), ('fmask', _c_void_p), ('fbits', _c_void_p),
+                ('terms', Terms), ('gofs', _c_void_p), ('dgrp', _c_void_p), ('diag0', _c_void_p),
+                ('rowptr', _c_void_p), ('col', _c_void_p), ('grp', _c_void_p),
+                ('nnz', ctypes.c_int64), ('states_size', _c_void_p)]
+
+
+BATCH_STATE_BITS = 40
+
 # name -> (restype, argtypes); mirrors include/rqsqd.h
 _P = ctypes.POINTER
 SIGNATURES = {
@@ -85,6 +97,14 @@ SIGNATURES = {
     'rq_lobpcg_solve_noalloc': (ctypes.c_int, [_P(Operator), _P(LobpcgParams), _c_void_p,
                                                _c_void_p, _P(LobpcgResult), _c_void_p]),
     'rq_eigenpair_3x3': (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p]),
+    'rq_batch_build': (ctypes.c_int, [_P(Batch), _c_void_p, _c_void_p]),
+    'rq_batch_conn_build': (ctypes.c_int, [_P(Batch), _c_void_p, _c_void_p, _c_void_p,
+                                           _P(ctypes.c_int64), _c_void_p, _c_void_p]),
+    'rq_batch_matvec': (ctypes.c_int, [_P(Batch), ctypes.c_int32, _c_void_p, _c_void_p, _c_void_p,
+                                       _c_void_p]),
+    'rq_batch_workspace_size': (ctypes.c_int, [_P(Batch), _P(LobpcgParams), _P(ctypes.c_size_t)]),
+    'rq_batch_solve': (ctypes.c_int, [_P(Batch), _P(LobpcgParams), _c_void_p, _c_void_p, _c_void_p,
+                                      _P(LobpcgResult), _c_void_p]),
     'rq_last_error': (ctypes.c_char_p, []),
     'rq_version': (ctypes.c_int, []),
 }

@@ -1212,3 +1212,173 @@ RQ_API int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_para
     p.use_graph = 0;
     return solve_entry(op, nullptr, nullptr, &p, ws, x0, x_out, res, stream);
 }
+
+// ------------------------------------------------------------------------------------------
+// Batched solve: every problem's rows in one vector, chunked segments, per-problem state
+// ------------------------------------------------------------------------------------------
+namespace rq {
+
+int batch_matvec_dispatch(const rq_batch_t &B, int32_t vt, const void *x, void *y, void *scratch,
+                          cudaStream_t st, const int *gate, int64_t gstride, const int *gate2);
+
+namespace {
+
+constexpr int64_t kBatchChunk = 2048;  // rows per block of the batched passes
+
+struct MvBatch {
+    const rq_batch_t *b;
+    void *scratch;
+    int operator()(int32_t vt, const void *in, void *out, cudaStream_t s, State *states,
+                   bool refresh) const {
+        return batch_matvec_dispatch(*b, vt, in, out, scratch, s, &states[0].active,
+                                     (int64_t)sizeof(State),
+                                     refresh ? &states[0].want_refresh : nullptr);
+    }
+};
+
+struct BatchPlan {
+    std::vector<int64_t> prow;
+    std::vector<int32_t> cprob, cofs;
+    std::vector<int64_t> crow;
+    size_t states, err, part, counter, tcprob, tcrow, tcofs, vec_hi, vec_lo, total;
+    size_t hi_bytes, lo_bytes;
+};
+
+int plan_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, BatchPlan &pl) {
+    const int P = b.P;
+    pl.prow.resize(P + 1);
+    RQ_CUDA(cudaMemcpy(pl.prow.data(), b.prow, sizeof(int64_t) * (P + 1), cudaMemcpyDeviceToHost));
+    if (pl.prow[0] != 0 || pl.prow[P] != b.D) return fail(RQ_E_ARG, "rq_batch: prow must span [0, D]");
+    pl.cofs.assign(1, 0);
+    for (int q = 0; q < P; ++q) {
+        const int64_t a = pl.prow[q], e = pl.prow[q + 1];
+        if (e <= a) return fail(RQ_E_ARG, "rq_batch: every problem needs at least one row");
+        for (int64_t r = a; r < e; r += kBatchChunk) {
+            pl.cprob.push_back(q);
+            pl.crow.push_back(r);
+        }
+        pl.cofs.push_back((int32_t)pl.cprob.size());
+    }
+    pl.crow.push_back(b.D);
+    const size_t nch = pl.cprob.size();
+    size_t off = 0;
+    auto take = [&](size_t n) {
+        size_t o = off;
+        off += (n + 255) & ~size_t(255);
+        return o;
+    };
+    pl.states = take(sizeof(State) * P);
+    pl.err = take(16);
+    pl.part = take(sizeof(double2) * kMaxReduce * nch);
+    pl.counter = take(sizeof(unsigned int) * P);
+    pl.tcprob = take(sizeof(int32_t) * nch);
+    pl.tcrow = take(sizeof(int64_t) * (nch + 1));
+    pl.tcofs = take(sizeof(int32_t) * (P + 1));
+    pl.hi_bytes = (size_t)b.D * vtype_size(p.vtype);
+    pl.lo_bytes = (size_t)b.D * vtype_size(lo_type(p.vtype));
+    pl.vec_hi = take(8 * ((pl.hi_bytes + 255) & ~size_t(255)));
+    pl.vec_lo = p.mixed ? take(8 * ((pl.lo_bytes + 255) & ~size_t(255))) : 0;
+    pl.total = off;
+    return RQ_OK;
+}
+
+template <typename VLO, typename VHI>
+int solve_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, const BatchPlan &pl, char *ws,
+                const void *x0, void *xout, rq_lobpcg_result_t *res, cudaStream_t s) {
+    const int P = b.P;
+    State *states = reinterpret_cast<State *>(ws + pl.states);
+    int *nactive = reinterpret_cast<int *>(ws + pl.err + 8);
+    unsigned int *counter = reinterpret_cast<unsigned int *>(ws + pl.counter);
+    int32_t *cprob = reinterpret_cast<int32_t *>(ws + pl.tcprob);
+    int64_t *crow = reinterpret_cast<int64_t *>(ws + pl.tcrow);
+    int32_t *cofs = reinterpret_cast<int32_t *>(ws + pl.tcofs);
+    RQ_CUDA(cudaMemsetAsync(ws + pl.err, 0, 16, s));
+    RQ_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int) * P, s));
+    RQ_CUDA(cudaMemcpyAsync(cprob, pl.cprob.data(), sizeof(int32_t) * pl.cprob.size(),
+                            cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(crow, pl.crow.data(), sizeof(int64_t) * pl.crow.size(),
+                            cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(cofs, pl.cofs.data(), sizeof(int32_t) * pl.cofs.size(),
+                            cudaMemcpyHostToDevice, s));
+    std::vector<double> tol_dim(P);
+    for (int q = 0; q < P; ++q) {
+        const int64_t rows = pl.prow[q + 1] - pl.prow[q];
+        if (b.states_size && b.states_size[q] < rows)
+            return fail(RQ_E_ARG, "rq_batch_solve: states_size below a problem's row count");
+        tol_dim[q] = (double)(b.states_size ? b.states_size[q] : rows);
+    }
+    const int32_t hi_type = p.vtype;
+    const double tol = p.tol > 0 ? p.tol : eps_of(hi_type);
+    const bool mixed = p.mixed && lo_type(hi_type) != hi_type;
+    const int grid = (int)pl.cprob.size();
+    SegBatch seg{states, cprob, crow, cofs, reinterpret_cast<double2 *>(ws + pl.part), counter};
+    void *mvscratch = ws + pl.err - kScratchErr;
+    const bool jac = p.jacobi != 0;
+    Phase<VHI, SegBatch, MvBatch> hi{MvBatch{&b, mvscratch}, hi_type, seg, grid, states, P, nactive,
+                                     carve_vecs<VHI>(ws + pl.vec_hi, pl.hi_bytes), jac, b.diag0};
+    Phase<VLO, SegBatch, MvBatch> lo{MvBatch{&b, mvscratch}, lo_type(hi_type), seg, grid, states, P,
+                                     nactive,
+                                     carve_vecs<VLO>(ws + (mixed ? pl.vec_lo : pl.vec_hi), pl.lo_bytes),
+                                     jac, b.diag0};
+    std::vector<int> nlo;
+    RQ_TRY(run_phases(lo, hi, mixed, p, tol, tol_dim, b.D, x0, pl.hi_bytes, kChunk,
+                      p.use_graph != 0, s, nlo));
+    std::vector<State> h(P);
+    int mv_err = 0;
+    RQ_CUDA(cudaMemcpyAsync(h.data(), states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaMemcpyAsync(&mv_err, ws + pl.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaMemcpyAsync(xout, hi.v.x, pl.hi_bytes, cudaMemcpyDeviceToDevice, s));
+    RQ_CUDA(cudaStreamSynchronize(s));
+    if (mv_err) return fail(mv_err, "rq_batch_solve: matvec reported an error");
+    for (int q = 0; q < P; ++q) fill_result(h[q], nlo[q], p, res + q);
+    return RQ_OK;
+}
+
+}  // namespace
+}  // namespace rq
+
+RQ_API int rq_batch_workspace_size(const rq_batch_t *b, const rq_lobpcg_params_t *prm,
+                                   size_t *bytes) {
+    if (!b || !prm || !bytes || !b->prow || b->P < 1)
+        return fail(RQ_E_ARG, "rq_batch_workspace_size: bad arguments");
+    if (vtype_size(prm->vtype) == 0) return fail(RQ_E_ARG, "rq_batch_workspace_size: bad vtype");
+    BatchPlan pl;
+    RQ_TRY(plan_batch(*b, *prm, pl));
+    *bytes = pl.total;
+    return RQ_OK;
+}
+
+RQ_API int rq_batch_solve(const rq_batch_t *b, const rq_lobpcg_params_t *prm, void *workspace,
+                          const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream) {
+    if (!b || !prm || !workspace || !x0 || !x_out || !res)
+        return fail(RQ_E_ARG, "rq_batch_solve: null argument");
+    if (prm->maxiter < 0 || (prm->variant != RQ_LOBPCG_REFERENCE && prm->variant != RQ_LOBPCG_FAST))
+        return fail(RQ_E_ARG, "rq_batch_solve: bad maxiter or variant");
+    const int32_t vt = prm->vtype;
+    if ((vt == RQ_F32 || vt == RQ_F64) && !b->terms.is_real)
+        return fail(RQ_E_ARG, "rq_batch_solve: real vectors need real coefficients");
+    BatchPlan pl;
+    RQ_TRY(plan_batch(*b, *prm, pl));
+    std::memset(res, 0, sizeof(rq_lobpcg_result_t) * b->P);
+    cudaStream_t user = as_stream(stream);
+    cudaStream_t s = user, priv = nullptr;
+    if (prm->use_graph && user == nullptr) {
+        RQ_CUDA(cudaStreamCreateWithFlags(&priv, cudaStreamNonBlocking));
+        RQ_CUDA(cudaDeviceSynchronize());
+        s = priv;
+    }
+    char *ws = static_cast<char *>(workspace);
+    int rc;
+    switch (vt) {
+        case RQ_F32: rc = solve_batch<float, float>(*b, *prm, pl, ws, x0, x_out, res, s); break;
+        case RQ_F64: rc = solve_batch<float, double>(*b, *prm, pl, ws, x0, x_out, res, s); break;
+        case RQ_C64: rc = solve_batch<float2, float2>(*b, *prm, pl, ws, x0, x_out, res, s); break;
+        case RQ_C128: rc = solve_batch<float2, double2>(*b, *prm, pl, ws, x0, x_out, res, s); break;
+        default: rc = fail(RQ_E_ARG, "rq_batch_solve: bad vtype");
+    }
+    if (priv) {
+        cudaStreamSynchronize(priv);
+        cudaStreamDestroy(priv);
+    }
+    return rc;
+}

@@ -737,6 +737,16 @@ int check_operator(const rq_operator_t *op, int32_t vtype) {
 
 }  // namespace
 
+// Inclusive scan of D row counts in place (block scans, scan of block totals, offsets).
+int scan_row_counts(int64_t *v, int64_t D, int64_t *bsum, cudaStream_t st) {
+    const int64_t nb = (D + 1023) / 1024;
+    k_scan_blocks<<<(int)nb, kThreads, 0, st>>>(v, D, bsum);
+    k_scan_totals<<<1, kThreads, 0, st>>>(bsum, nb);
+    k_scan_add<<<(int)nb, kThreads, 0, st>>>(v, D, bsum);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
+}
+
 // entry used by the LOBPCG driver (same translation-unit-independent dispatch)
 int matvec_dispatch(const rq_operator_t &op, int32_t vtype, const void *x, void *y, void *scratch,
                     cudaStream_t st, const int *gate, const int *gate2) {
@@ -816,12 +826,7 @@ RQ_API int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col,
         else
             k_conn_count<RQ_LOOKUP_BSEARCH, 64><<<grid_rows(D), kThreads, 0, st>>>(*op, rowptr + 1, err);
         RQ_CUDA(cudaGetLastError());
-        const int64_t nb = (D + 1023) / 1024;
-        int64_t *bsum = scratch_scan(scratch);
-        k_scan_blocks<<<(int)nb, kThreads, 0, st>>>(rowptr + 1, D, bsum);
-        k_scan_totals<<<1, kThreads, 0, st>>>(bsum, nb);
-        k_scan_add<<<(int)nb, kThreads, 0, st>>>(rowptr + 1, D, bsum);
-        RQ_CUDA(cudaGetLastError());
+        RQ_TRY(scan_row_counts(rowptr + 1, D, scratch_scan(scratch), st));
         int h_err = 0;
         RQ_CUDA(cudaMemcpyAsync(nnz, rowptr + D, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         RQ_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));

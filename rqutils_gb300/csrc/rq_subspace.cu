@@ -2,6 +2,8 @@
 //   rq_subspace_build  -- strict-increase check, empty-key choice, hash table, sector filter
 //   rq_xsource         -- get_xsource (rqutils/sqd.py:448-503) for any number of X masks
 //   rq_diagonal        -- get_diagonal (rqutils/sqd.py:554-575), stopping at the first zero
+#include <string>
+
 #include "rq_common.cuh"
 #include "rq_host.h"
 
@@ -182,6 +184,63 @@ int grid_for(int64_t n, int per_sm = 8) {
 
 }  // namespace
 
+// Strict-increase check, empty-key choice and hash insertion for a sorted key array; shared by
+// rq_subspace_build and rq_batch_build.  `flag` and `gap` are device scratch words.
+int build_key_table(const uint64_t *keys, int64_t D, int key_bits, bool hash, void *hkeys,
+                    int32_t *hvals, int hbits, uint64_t *empty_out, int *flag,
+                    unsigned long long *gap, cudaStream_t st) {
+    RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    RQ_CUDA(cudaMemsetAsync(gap, 0xff, sizeof(unsigned long long), st));
+    k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(keys, D, flag);
+    RQ_CUDA(cudaGetLastError());
+    int h_flag = 0;
+    unsigned long long h_gap = 0;
+    uint64_t first = 0, last = 0;
+    RQ_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaMemcpyAsync(&first, keys, 8, cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaMemcpyAsync(&last, keys + (D - 1), 8, cudaMemcpyDeviceToHost, st));
+    RQ_CUDA(cudaStreamSynchronize(st));
+    if (h_flag) return fail(RQ_E_UNSORTED, "keys are not strictly increasing");
+    const uint64_t top = key_bits == 32 ? 0xFFFFFFFFULL : ~0ULL;
+    if (key_bits == 32 && last > top)
+        return fail(RQ_E_RANGE, "key_bits = 32 needs every state < 2^32");
+    uint64_t empty;
+    if (last != top) {
+        empty = top;
+    } else if (first != 0ULL) {
+        empty = 0ULL;
+    } else {  // both extremes present: the first gap exists because D < 2^64
+        k_first_gap<<<grid_for(D), kThreads, 0, st>>>(keys, D, gap);
+        RQ_CUDA(cudaMemcpyAsync(&h_gap, gap, sizeof(h_gap), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaStreamSynchronize(st));
+        uint64_t below = 0;
+        RQ_CUDA(cudaMemcpy(&below, keys + h_gap, 8, cudaMemcpyDeviceToHost));
+        empty = below + 1;
+    }
+    *empty_out = empty;
+    RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (hash) {
+        const int64_t nslots = int64_t(kBucketSlots) << hbits;
+        if (key_bits == 64) {
+            k_fill_u64<<<grid_for(nslots), kThreads, 0, st>>>(static_cast<uint64_t *>(hkeys), nslots,
+                                                              empty);
+            k_hash_insert<64><<<grid_for(D), kThreads, 0, st>>>(keys, D, hkeys, hvals, hbits, empty,
+                                                                flag);
+        } else {
+            k_fill_u32<<<grid_for(nslots), kThreads, 0, st>>>(static_cast<uint32_t *>(hkeys), nslots,
+                                                              (uint32_t)empty);
+            k_hash_insert<32><<<grid_for(D), kThreads, 0, st>>>(keys, D, hkeys, hvals, hbits, empty,
+                                                                flag);
+        }
+        RQ_CUDA(cudaGetLastError());
+        int h_err = 0;
+        RQ_CUDA(cudaMemcpyAsync(&h_err, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaStreamSynchronize(st));
+        if (h_err) return fail(RQ_E_TABLE, "hash insertion failed");
+    }
+    return RQ_OK;
+}
+
 }  // namespace rq
 
 using namespace rq;
@@ -216,59 +275,15 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     cudaStream_t st = as_stream(stream);
     int *flag = scratch_err(scratch);
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
-    RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    RQ_CUDA(cudaMemsetAsync(gap, 0xff, sizeof(unsigned long long), st));
-    k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, flag);
-    RQ_CUDA(cudaGetLastError());
-    int h_flag = 0;
-    unsigned long long h_gap = 0;
-    uint64_t first = 0, last = 0;
-    RQ_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RQ_CUDA(cudaMemcpyAsync(&h_gap, gap, sizeof(h_gap), cudaMemcpyDeviceToHost, st));
-    RQ_CUDA(cudaMemcpyAsync(&first, sub->states, 8, cudaMemcpyDeviceToHost, st));
-    RQ_CUDA(cudaMemcpyAsync(&last, sub->states + (D - 1), 8, cudaMemcpyDeviceToHost, st));
-    RQ_CUDA(cudaStreamSynchronize(st));
-    if (h_flag) return fail(RQ_E_UNSORTED, "rq_subspace_build: states are not strictly increasing");
-    const uint64_t top = sub->key_bits == 32 ? 0xFFFFFFFFULL : ~0ULL;
-    if (sub->key_bits == 32 && last > top)
-        return fail(RQ_E_RANGE, "rq_subspace_build: key_bits = 32 needs every state < 2^32");
-    uint64_t empty;
-    if (last != top) {
-        empty = top;
-    } else if (first != 0ULL) {
-        empty = 0ULL;
-    } else {  // both extremes present: the first gap exists because D < 2^64
-        k_first_gap<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, gap);
-        RQ_CUDA(cudaMemcpyAsync(&h_gap, gap, sizeof(h_gap), cudaMemcpyDeviceToHost, st));
-        RQ_CUDA(cudaStreamSynchronize(st));
-        uint64_t below = 0;
-        RQ_CUDA(cudaMemcpy(&below, sub->states + h_gap, 8, cudaMemcpyDeviceToHost));
-        empty = below + 1;
-    }
-    sub->empty_key = empty;
-    RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
-    if (sub->lookup == RQ_LOOKUP_HASH) {
-        const int64_t nslots = int64_t(slots) << sub->hbits;
-        if (sub->key_bits == 64) {
-            k_fill_u64<<<grid_for(nslots), kThreads, 0, st>>>(static_cast<uint64_t *>(sub->hkeys),
-                                                              nslots, empty);
-            k_hash_insert<64><<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->hkeys,
-                                                                sub->hvals, sub->hbits, empty, flag);
-        } else {
-            k_fill_u32<<<grid_for(nslots), kThreads, 0, st>>>(static_cast<uint32_t *>(sub->hkeys),
-                                                              nslots, (uint32_t)empty);
-            k_hash_insert<32><<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->hkeys,
-                                                                sub->hvals, sub->hbits, empty, flag);
-        }
-        RQ_CUDA(cudaGetLastError());
-    }
+    const int rc = build_key_table(sub->states, D, sub->key_bits, sub->lookup == RQ_LOOKUP_HASH,
+                                   sub->hkeys, sub->hvals, sub->hbits, &sub->empty_key, flag, gap,
+                                   st);
+    if (rc != RQ_OK) return fail(rc, std::string("rq_subspace_build: ") + rq_last_error());
     RQ_CUDA(cudaMemsetAsync(sub->fbits, 0, RQ_FILTER_WORDS * sizeof(uint32_t), st));
     k_filter_build<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->fmask_a, sub->fmask_b,
                                                       sub->fbits);
     RQ_CUDA(cudaGetLastError());
-    RQ_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     RQ_CUDA(cudaStreamSynchronize(st));
-    if (h_flag) return fail(RQ_E_TABLE, "rq_subspace_build: hash insertion failed");
     return RQ_OK;
 }
 

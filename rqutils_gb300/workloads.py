@@ -35,6 +35,49 @@ def random_pauli_sum(rng, n, K, locality=(1, 4)):
     return paulis, coeffs
 
 
+def random_pauli_masks(rng, n, K, locality=(1, 4)):
+    """Vectorised random real Pauli sum: K terms of weight uniform in ``locality`` on distinct
+    random qubits, letters uniform in X/Y/Z, coefficients N(0, 1).  Returns ([str] * K, (K,))."""
+    lo, hi = locality
+    w = rng.integers(lo, hi + 1, size=K)
+    order = np.argsort(rng.random((K, n)), axis=1)          # a random permutation per term
+    pick = np.arange(n)[None, :] < w[:, None]                  # its first w qubits
+    letter = rng.integers(1, 4, size=(K, n))                  # 1 = X, 2 = Z, 3 = Y
+    bit = np.left_shift(np.uint64(1), order.astype(np.uint64))
+    xb = np.where(pick & (letter != 2), bit, np.uint64(0))
+    zb = np.where(pick & (letter != 1), bit, np.uint64(0))
+    x = np.bitwise_or.reduce(xb, axis=1)
+    z = np.bitwise_or.reduce(zb, axis=1)
+    return xz_labels(x, z, n), rng.normal(0., 1., size=K)
+
+
+def batched_random_problems(seed, P=256, n_range=(16, 40), k_range=(100, 2000),
+                            d_range=(2 ** 10, 2 ** 18)):
+    """P independent random Pauli-sum SQD problems: N uniform in ``n_range``, K log-uniform in
+    ``k_range``, D log-uniform in ``d_range`` (capped at half the sector), states of Hamming
+    weight N // 2 (one block for N <= 32; above, a product of two half-width blocks).  Returns
+    (paulisums [(labels, coeffs)], states [sorted uint64], nqubits)."""
+    rng = np.random.default_rng(seed)
+    hams, states, ns = [], [], []
+    for _ in range(P):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        K = int(np.exp(rng.uniform(np.log(k_range[0]), np.log(k_range[1]))))
+        D = int(np.exp(rng.uniform(np.log(d_range[0]), np.log(d_range[1]))))
+        w = n // 2
+        if n <= 32:
+            blocks = [(n, w)]
+        else:
+            blocks = [(n // 2, w // 2), (n - n // 2, w - w // 2)]
+        total = 1
+        for nb, ww in blocks:
+            total *= _comb(nb, ww)
+        D = max(1, min(D, total // 2))
+        hams.append(random_pauli_masks(rng, n, K))
+        states.append(sample_sector(rng, D, blocks))
+        ns.append(n)
+    return hams, states, ns
+
+
 def _string(n, ops):
     """Pauli string of length n from {qubit: 'X'|'Y'|'Z'}."""
     row = ['I'] * n

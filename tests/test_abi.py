@@ -69,3 +69,5 @@ def test_struct_layouts():
     assert ctypes.sizeof(L.Operator) == 80 + 56 + 8 + 40 + 8
     assert ctypes.sizeof(L.LobpcgParams) == 64
     assert ctypes.sizeof(L.LobpcgResult) == 48
+    assert ctypes.sizeof(L.Batch) == 200
+    assert L.Batch.terms.offset == 80 and L.Batch.nnz.offset == 184

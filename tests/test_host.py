@@ -150,3 +150,41 @@ def test_chemistry_truncation_keeps_largest():
     full_l, full_c = workloads.chemistry_jw(4, np.random.default_rng(1))
     assert len(labels) == 50
     assert np.min(np.abs(coeffs)) >= np.sort(np.abs(full_c))[-50] - 1e-15
+
+
+def test_batch_composite_keys_and_terms():
+    """Host layout of a batch: composite keys sorted by (problem, state), row and group ranges
+    consistent with each problem's own grouped terms."""
+    from rqutils_gb300.batch import STATE_BITS, composite_keys, concat_terms
+    hams_raw, states, ns = workloads.batched_random_problems(3, P=6, d_range=(16, 300),
+                                                             k_range=(10, 60))
+    hams = [PauliSumXZ.from_paulisum(h, force_real=True, add_padding=True) for h in hams_raw]
+    keys, prow = composite_keys(states)
+    assert np.all(keys[1:] > keys[:-1])
+    assert prow[0] == 0 and prow[-1] == len(keys)
+    for p, s in enumerate(states):
+        seg = keys[prow[p]:prow[p + 1]]
+        assert np.all((seg >> np.uint64(STATE_BITS)) == p)
+        np.testing.assert_array_equal(seg & np.uint64((1 << STATE_BITS) - 1), s)
+    xm, toff, zm, cf, gofs, dgrp, real = concat_terms(hams)
+    for p, h in enumerate(hams):
+        x1, t1, z1, c1, dg1, _ = h.device_arrays(truncate=True)
+        g0, g1 = gofs[p], gofs[p + 1]
+        np.testing.assert_array_equal(xm[g0:g1], x1)
+        np.testing.assert_array_equal(toff[g0:g1 + 1] - toff[g0], t1)
+        np.testing.assert_array_equal(zm[toff[g0]:toff[g1]], z1)
+        np.testing.assert_array_equal(cf[toff[g0]:toff[g1]], c1)
+        assert dgrp[p] == (g0 + dg1 if dg1 >= 0 else -1)
+    with pytest.raises(ValueError):
+        composite_keys([np.array([1 << STATE_BITS], np.uint64)])
+
+
+def test_batched_random_problems_shapes():
+    hams, states, ns = workloads.batched_random_problems(4, P=12, d_range=(2 ** 6, 2 ** 10),
+                                                         k_range=(100, 200))
+    for (lab, c), s, n in zip(hams, states, ns):
+        assert 16 <= n <= 40 and len(lab[0]) == n
+        assert 100 <= len(lab) <= 200
+        assert np.all(s[1:] > s[:-1])
+        assert np.all(np.bitwise_count(s) == n // 2)
+        assert 1 <= len(s) <= 2 ** 10
