@@ -134,6 +134,16 @@ int rq_xsource(const rq_subspace_t *sub, const uint64_t *xmask, int32_t J, int32
 int rq_diagonal(const uint64_t *states, int64_t D, const uint64_t *zmask, const double *coef,
                 int32_t K, double *out, void *stream);
 
+/* Upload grouped terms from HOST arrays (X masks strictly increasing, group offsets toff[J+1]
+ * from 0 to K, coefficients interleaved re/im) into caller-owned device buffers d_xmask[J],
+ * d_toff[J+1], d_zmask[K], d_coef[2K], d_xhash[J]; fill *t (J, K, diag_group, is_real, the
+ * device pointers) and compute the X hashes.  The device form of PauliSumXZ
+ * (symplectic.py:42-49).  Synchronises the stream; the host arrays may be freed on return. */
+int rq_terms_upload(int32_t J, int32_t K, const uint64_t *xmask, const int32_t *toff,
+                    const uint64_t *zmask, const double *coef, uint64_t *d_xmask, int32_t *d_toff,
+                    uint64_t *d_zmask, double *d_coef, uint32_t *d_xhash, rq_terms_t *t,
+                    void *stream);
+
 /* Fill xhash[j] with the lookup hash of xmask[j] (used by RQ_LOOKUP_HASH matvecs: a row's
  * target bucket is hash(row) ^ xhash[j]).  Setup call, stream-ordered. */
 int rq_terms_hash(const rq_terms_t *terms, uint32_t *xhash, void *stream);
@@ -271,6 +281,64 @@ int rq_batch_matvec(const rq_batch_t *b, int32_t vtype, const void *x, void *y, 
 int rq_batch_workspace_size(const rq_batch_t *b, const rq_lobpcg_params_t *prm, size_t *bytes);
 int rq_batch_solve(const rq_batch_t *b, const rq_lobpcg_params_t *prm, void *workspace,
                    const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
+
+/* ---- learned warm start ------------------------------------------------------------------
+ * An MLP f(features) -> (log-amplitude, sign logit) of the ground state, trained on ground
+ * states of related problems (the same subspace, another value of a Hamiltonian parameter U)
+ * and evaluated on every state of a new problem to give LOBPCG its start vector (replaces the
+ * one-hot start of sqd.py:373-398).  Architecture: 64 inputs (the 32 low state bits as +-1,
+ * then (U - 5) / 3, its square and cube, zeros), two hidden layers of 256 GELU units, 2
+ * outputs.  BF16 weights and activations on the tcgen05 tensor cores (FP32 accumulators in
+ * TMEM), FP32 master weights and Adam state.  Row counts of rq_mlp_bwd are multiples of 128. */
+
+#define RQ_MLP_IN 64
+#define RQ_MLP_HIDDEN 256
+#define RQ_MLP_OUT 2
+#define RQ_MLP_NPARAMS (256 * 64 + 256 + 256 * 256 + 256 + 2 * 256 + 2)
+
+typedef struct rq_mlp {
+    float    *params;     /* [NPARAMS] FP32: W1[256][64] b1[256] W2[256][256] b2[256] W3[2][256] b3[2] */
+    float    *grads;      /* [NPARAMS] written by rq_mlp_bwd (same layout)                      */
+    float    *adam_m;     /* [NPARAMS] Adam first moment                                         */
+    float    *adam_v;     /* [NPARAMS] Adam second moment                                        */
+    uint16_t *w1b;        /* [256][64]  BF16 copy of W1     (rq_mlp_sync / rq_mlp_step)          */
+    uint16_t *w2b;        /* [256][256] BF16 copy of W2                                          */
+    uint16_t *w2tb;       /* [256][256] BF16 copy of W2 transposed                               */
+} rq_mlp_t;
+
+/* Device workspace of rq_mlp_fwd / rq_mlp_bwd for `rows` rows (activations kept for bwd). */
+int rq_mlp_workspace_size(int64_t rows, size_t *bytes);
+/* Refresh the BF16 weight copies from params. */
+int rq_mlp_sync(const rq_mlp_t *m, void *stream);
+/* Features of every state for one U: x[D][64] BF16. */
+int rq_mlp_features(const uint64_t *states, int64_t D, double U, uint16_t *x, void *stream);
+/* Training minibatch: `rows` pairs (problem i, row k) drawn by a counter-based hash of
+ * (seed, step, row); features x[rows][64] and xt[64][rows] (BF16), targets tgt[rows][3] =
+ * (log(sqrt(D) |psi_i[k]|), sign psi_i[k], weight clamp(D psi_i[k]^2, 0.05, 20)).
+ * psi is [P][D] FP32 (each ground state normalised), U is [P]. */
+int rq_mlp_sample(const uint64_t *states, int64_t D, const double *U, const float *psi, int32_t P,
+                  uint64_t seed, int64_t step, int64_t rows, uint16_t *x, uint16_t *xt, float *tgt,
+                  void *stream);
+/* out[rows][2] = f(x); keeps the activations in ws for rq_mlp_bwd. */
+int rq_mlp_fwd(const rq_mlp_t *m, int64_t rows, const uint16_t *x, float *out, void *ws,
+               void *stream);
+/* dout[rows][2] of the weighted loss mean_i w_i ((o0 - a_i)^2 + softplus(-s_i o1)); the loss
+ * itself is written to loss[0] (device double) when loss is not NULL. */
+int rq_mlp_loss(int64_t rows, const float *out, const float *tgt, float *dout, double *loss,
+                void *ws, void *stream);
+/* m->grads = d loss / d params from dout and the activations of the last rq_mlp_fwd on ws. */
+int rq_mlp_bwd(const rq_mlp_t *m, int64_t rows, const uint16_t *xt, const float *dout, void *ws,
+               void *stream);
+/* One Adam step (step number t >= 1) on params from grads; refreshes the BF16 copies. */
+int rq_mlp_step(const rq_mlp_t *m, int32_t t, float lr, float beta1, float beta2, float eps,
+                void *stream);
+/* Start vector x0[k] = sign(o1_k) exp(o0_k) of value type vtype from out[D][2]. */
+int rq_mlp_warm_start(int64_t D, const float *out, int32_t vtype, void *x0, void *stream);
+/* The tensor-core GEMM under the MLP: C[M][N] = A[M][K] B[N][K]^T (BF16 in, FP32 out), N 64 or
+ * 256, K a multiple of 64, row strides multiples of 8 elements; ws: 16 bytes of device memory
+ * (error flag). */
+int rq_bf16_gemm(const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb, int64_t M,
+                 int32_t N, int64_t K, float *C, void *ws, void *stream);
 
 /* ---- diagnostics ------------------------------------------------------------------------- */
 

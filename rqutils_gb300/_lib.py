@@ -70,6 +70,14 @@ class Batch(ctypes.Structure):
 
 
 BATCH_STATE_BITS = 40
+MLP_IN, MLP_HIDDEN, MLP_OUT = 64, 256, 2
+MLP_NPARAMS = 256 * 64 + 256 + 256 * 256 + 256 + 2 * 256 + 2
+
+
+class Mlp(ctypes.Structure):
+    _fields_ = [('params', _c_void_p), ('grads', _c_void_p), ('adam_m', _c_void_p),
+                ('adam_v', _c_void_p), ('w1b', _c_void_p), ('w2b', _c_void_p),
+                ('w2tb', _c_void_p)]
 
 # name -> (restype, argtypes); mirrors include/rqsqd.h
 _P = ctypes.POINTER
@@ -80,6 +88,9 @@ SIGNATURES = {
     'rq_xsource': (ctypes.c_int, [_P(Subspace), _c_void_p, ctypes.c_int32, _c_void_p, _c_void_p]),
     'rq_diagonal': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, _c_void_p,
                                    ctypes.c_int32, _c_void_p, _c_void_p]),
+    'rq_terms_upload': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _c_void_p, _c_void_p,
+                                       _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
+                                       _c_void_p, _c_void_p, _P(Terms), _c_void_p]),
     'rq_terms_hash': (ctypes.c_int, [_P(Terms), _c_void_p, _c_void_p]),
     'rq_conn_build': (ctypes.c_int, [_P(Operator), _c_void_p, _c_void_p, _c_void_p, _c_void_p,
                                      ctypes.c_int32, _P(ctypes.c_int64), _c_void_p, _c_void_p]),
@@ -105,6 +116,26 @@ SIGNATURES = {
     'rq_batch_workspace_size': (ctypes.c_int, [_P(Batch), _P(LobpcgParams), _P(ctypes.c_size_t)]),
     'rq_batch_solve': (ctypes.c_int, [_P(Batch), _P(LobpcgParams), _c_void_p, _c_void_p, _c_void_p,
                                       _P(LobpcgResult), _c_void_p]),
+    'rq_mlp_workspace_size': (ctypes.c_int, [ctypes.c_int64, _P(ctypes.c_size_t)]),
+    'rq_mlp_sync': (ctypes.c_int, [_P(Mlp), _c_void_p]),
+    'rq_mlp_features': (ctypes.c_int, [_c_void_p, ctypes.c_int64, ctypes.c_double, _c_void_p,
+                                       _c_void_p]),
+    'rq_mlp_sample': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, _c_void_p,
+                                     ctypes.c_int32, ctypes.c_uint64, ctypes.c_int64,
+                                     ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
+    'rq_mlp_fwd': (ctypes.c_int, [_P(Mlp), ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
+                                  _c_void_p]),
+    'rq_mlp_loss': (ctypes.c_int, [ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
+                                   _c_void_p, _c_void_p]),
+    'rq_mlp_bwd': (ctypes.c_int, [_P(Mlp), ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
+                                  _c_void_p]),
+    'rq_mlp_step': (ctypes.c_int, [_P(Mlp), ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_float, ctypes.c_float, _c_void_p]),
+    'rq_mlp_warm_start': (ctypes.c_int, [ctypes.c_int64, _c_void_p, ctypes.c_int32, _c_void_p,
+                                         _c_void_p]),
+    'rq_bf16_gemm': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, ctypes.c_int64,
+                                    ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, _c_void_p,
+                                    _c_void_p, _c_void_p]),
     'rq_last_error': (ctypes.c_char_p, []),
     'rq_version': (ctypes.c_int, []),
 }

@@ -806,6 +806,46 @@ RQ_API int rq_terms_hash(const rq_terms_t *terms, uint32_t *xhash, void *stream)
     return RQ_OK;
 }
 
+RQ_API int rq_terms_upload(int32_t J, int32_t K, const uint64_t *xmask, const int32_t *toff,
+                           const uint64_t *zmask, const double *coef, uint64_t *d_xmask,
+                           int32_t *d_toff, uint64_t *d_zmask, double *d_coef, uint32_t *d_xhash,
+                           rq_terms_t *t, void *stream) {
+    if (!t || J < 0 || K < 0 || !toff || !d_toff || (J > 0 && (!xmask || !d_xmask || !d_xhash)) ||
+        (K > 0 && (!zmask || !coef || !d_zmask || !d_coef)))
+        return fail(RQ_E_ARG, "rq_terms_upload: bad arguments");
+    if (toff[0] != 0 || toff[J] != K) return fail(RQ_E_ARG, "rq_terms_upload: toff must span [0, K]");
+    for (int32_t j = 0; j < J; ++j) {
+        if (toff[j + 1] < toff[j]) return fail(RQ_E_ARG, "rq_terms_upload: toff decreases");
+        if (j > 0 && xmask[j] <= xmask[j - 1])
+            return fail(RQ_E_ARG, "rq_terms_upload: X masks must be strictly increasing");
+    }
+    int32_t real = 1;
+    for (int64_t k = 0; k < K; ++k)
+        if (coef[2 * k + 1] != 0.) real = 0;
+    cudaStream_t st = as_stream(stream);
+    if (J > 0) RQ_CUDA(cudaMemcpyAsync(d_xmask, xmask, sizeof(uint64_t) * J, cudaMemcpyHostToDevice, st));
+    RQ_CUDA(cudaMemcpyAsync(d_toff, toff, sizeof(int32_t) * (J + 1), cudaMemcpyHostToDevice, st));
+    if (K > 0) {
+        RQ_CUDA(cudaMemcpyAsync(d_zmask, zmask, sizeof(uint64_t) * K, cudaMemcpyHostToDevice, st));
+        RQ_CUDA(cudaMemcpyAsync(d_coef, coef, sizeof(double) * 2 * K, cudaMemcpyHostToDevice, st));
+    }
+    rq_terms_t T{};
+    T.J = J;
+    T.K = K;
+    T.diag_group = (J > 0 && xmask[0] == 0) ? 0 : -1;
+    T.is_real = real;
+    T.xmask = d_xmask;
+    T.toff = d_toff;
+    T.zmask = d_zmask;
+    T.coef = d_coef;
+    T.xhash = nullptr;
+    RQ_TRY(rq_terms_hash(&T, d_xhash, stream));
+    T.xhash = J > 0 ? d_xhash : nullptr;
+    RQ_CUDA(cudaStreamSynchronize(st));
+    *t = T;
+    return RQ_OK;
+}
+
 RQ_API int rq_conn_build(const rq_operator_t *op, int64_t *rowptr, int32_t *col, int32_t *grp,
                          void *val, int32_t vtype, int64_t *nnz, void *scratch, void *stream) {
     RQ_TRY(check_operator(op, val ? vtype : RQ_C128));

@@ -120,21 +120,25 @@ class DeviceTerms:
         self.diag_group = diag_group
         self.is_real = is_real
         self.num_qubits = ham.num_qubits
-        self.xmask = _u64_tensor(xmask, self.device)
-        self.toff = torch.from_numpy(np.ascontiguousarray(toff, dtype=np.int32)).to(self.device)
-        self.zmask = _u64_tensor(zmask if len(zmask) else np.zeros(1, np.uint64), self.device)
-        cf = np.ascontiguousarray(coef if len(coef) else np.zeros(1, np.complex128),
-                                  dtype=np.complex128)
-        self.coef = torch.from_numpy(cf.view(np.float64)).to(self.device)
+        dev = self.device
+        self.xmask = torch.empty(max(self.J, 1), dtype=torch.int64, device=dev)
+        self.toff = torch.empty(self.J + 1, dtype=torch.int32, device=dev)
+        self.zmask = torch.empty(max(self.K, 1), dtype=torch.int64, device=dev)
+        self.coef = torch.empty(2 * max(self.K, 1), dtype=torch.float64, device=dev)
+        self.xhash = torch.empty(max(self.J, 1), dtype=torch.int32, device=dev)
         self.group_sizes = np.diff(toff)
-        self.xhash = torch.empty(max(self.J, 1), dtype=torch.int32, device=self.device)
-        self.c = L.Terms(J=self.J, K=self.K, diag_group=diag_group, is_real=int(is_real),
-                         xmask=L.ptr(self.xmask), toff=L.ptr(self.toff), zmask=L.ptr(self.zmask),
-                         coef=L.ptr(self.coef), xhash=None)
-        if self.J:
-            L.check(L.lib().rq_terms_hash(ctypes.byref(self.c), L.ptr(self.xhash), L.stream_ptr()),
-                    'rq_terms_hash')
-            self.c.xhash = L.ptr(self.xhash)
+        xh = np.ascontiguousarray(xmask, dtype=np.uint64)
+        th = np.ascontiguousarray(toff, dtype=np.int32)
+        zh = np.ascontiguousarray(zmask, dtype=np.uint64)
+        ch = np.ascontiguousarray(coef, dtype=np.complex128)
+        self.c = L.Terms()
+        L.check(L.lib().rq_terms_upload(self.J, self.K, xh.ctypes.data, th.ctypes.data,
+                                        zh.ctypes.data, ch.ctypes.data, L.ptr(self.xmask),
+                                        L.ptr(self.toff), L.ptr(self.zmask), L.ptr(self.coef),
+                                        L.ptr(self.xhash), ctypes.byref(self.c), L.stream_ptr()),
+                'rq_terms_upload')
+        # the dtype rule of the reference (every phased coefficient real) over all terms
+        self.c.is_real = int(is_real)
 
 
 class DeviceOperator:

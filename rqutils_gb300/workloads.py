@@ -324,6 +324,33 @@ def sample_sector(rng, D, blocks):
     return have
 
 
+def low_double_occupancy_states(rng, D, Ns=16, n_up=None, n_dn=None):
+    """D distinct half-filled Hubbard configurations with at most one doubly occupied site, drawn
+    uniformly without replacement and sorted (bit i = site i up, bit Ns + i = site i down).  With
+    n_up = n_dn = Ns / 2 the pool is C(Ns, Ns/2) (1 + (Ns/2)^2) states (836,550 for 4x4); the
+    hopping terms connect a large part of it, unlike a uniform sample of the whole sector."""
+    n_up = Ns // 2 if n_up is None else n_up
+    n_dn = Ns - n_up if n_dn is None else n_dn
+    if n_up + n_dn != Ns:
+        raise ValueError('half filling: n_up + n_dn must equal the number of sites')
+    full = (1 << Ns) - 1
+    ups = _enumerate_sector([(Ns, n_up)])
+    comp = (~ups) & np.uint64(full)                 # down = complement: no double occupancy
+    pools = [ups | (comp << np.uint64(Ns))]
+    # one double: move one down electron from a hole of the up pattern onto an up site
+    bits = np.arange(Ns, dtype=np.uint64)
+    for a in range(Ns):
+        for b in range(Ns):
+            sel = ((ups >> bits[a]) & np.uint64(1)).astype(bool) & \
+                  ((comp >> bits[b]) & np.uint64(1)).astype(bool)
+            dn = (comp[sel] | (np.uint64(1) << bits[a])) & ~(np.uint64(1) << bits[b])
+            pools.append(ups[sel] | (dn << np.uint64(Ns)))
+    pool = np.concatenate(pools)
+    if D > len(pool):
+        raise ValueError(f'D={D} exceeds the pool of {len(pool)} configurations')
+    return np.sort(rng.choice(pool, size=D, replace=False))
+
+
 def sorted_unique(a):
     """Sorted distinct values of a 1-d array (sort + adjacent difference)."""
     a = np.sort(np.asarray(a))

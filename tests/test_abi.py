@@ -71,3 +71,24 @@ def test_struct_layouts():
     assert ctypes.sizeof(L.LobpcgResult) == 48
     assert ctypes.sizeof(L.Batch) == 200
     assert L.Batch.terms.offset == 80 and L.Batch.nnz.offset == 184
+    assert ctypes.sizeof(L.Mlp) == 56
+
+
+def test_terms_upload_validates_on_the_host(libpath):
+    """rq_terms_upload rejects a bad grouping before it touches the device."""
+    import numpy as np
+    from rqutils_gb300 import _lib as L
+    lib = L.lib()
+    t = L.Terms()
+    dummy = ctypes.c_void_p(16)  # never dereferenced: validation fails first
+    xm = np.array([3, 1], np.uint64)            # not increasing
+    toff = np.array([0, 1, 2], np.int32)
+    zm = np.zeros(2, np.uint64)
+    cf = np.zeros(4, np.float64)
+    args = [xm.ctypes.data, toff.ctypes.data, zm.ctypes.data, cf.ctypes.data] + [dummy] * 5
+    assert lib.rq_terms_upload(2, 2, *args, ctypes.byref(t), None) == L.E_ARG
+    assert b'increasing' in lib.rq_last_error()
+    xm2 = np.array([1, 3], np.uint64)
+    bad = np.array([0, 2, 1], np.int32)          # does not end at K
+    args = [xm2.ctypes.data, bad.ctypes.data, zm.ctypes.data, cf.ctypes.data] + [dummy] * 5
+    assert lib.rq_terms_upload(2, 2, *args, ctypes.byref(t), None) == L.E_ARG

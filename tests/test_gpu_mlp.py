@@ -1,0 +1,183 @@
+"""Tensor-core MLP of the learned warm start (rq_mlp_*, rq_bf16_gemm) against PyTorch FP32
+references of the same operations (same BF16 roundings)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from rqutils_gb300._build import build
+    build()
+
+
+def _gemm(A, B, K):
+    import ctypes
+    import torch
+    from rqutils_gb300 import _lib as L
+    M, N = A.shape[0], B.shape[0]
+    C = torch.empty((M, N), dtype=torch.float32, device='cuda')
+    ws = torch.zeros(64, dtype=torch.uint8, device='cuda')
+    L.check(L.lib().rq_bf16_gemm(L.ptr(A), A.stride(0), L.ptr(B), B.stride(0), M, N, K, L.ptr(C),
+                                 L.ptr(ws), L.stream_ptr()), 'rq_bf16_gemm')
+    torch.cuda.synchronize()
+    assert int(ws[:4].view(torch.int32).item()) == 0
+    return C
+
+
+@pytest.mark.parametrize('N', [64, 256])
+@pytest.mark.parametrize('M,K,lda', [(128, 64, 64), (300, 192, 192), (257, 128, 256)])
+def test_bf16_gemm_exact_on_small_integers(N, M, K, lda):
+    """Integer operands in [-3, 3]: every product and partial sum is exact in FP32, so the
+    tensor-core result must equal the FP32 product bit for bit (layouts, descriptors, K loop,
+    ragged row tile)."""
+    import torch
+    g = torch.Generator().manual_seed(M + N + K)
+    Afull = torch.randint(-3, 4, (M, lda), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randint(-3, 4, (N, K), generator=g).to(torch.bfloat16).cuda()
+    C = _gemm(Afull, B, K)
+    ref = Afull[:, :K].float() @ B.float().T
+    assert torch.equal(C, ref)
+
+
+def test_bf16_gemm_random_values():
+    import torch
+    g = torch.Generator().manual_seed(7)
+    A = torch.randn((1000, 512), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn((256, 512), generator=g).to(torch.bfloat16).cuda()
+    C = _gemm(A, B, 512)
+    ref = A.double() @ B.double().T
+    err = (C.double() - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+
+
+def _reference_forward(m, x):
+    import torch
+    import torch.nn.functional as F
+    W1, b1, W2, b2, W3, b3 = m.views()
+    z1 = x.float() @ m.w1b.float().T + b1
+    h1b = F.gelu(z1).to(torch.bfloat16).float()
+    z2 = h1b @ m.w2b.float().T + b2
+    out = F.gelu(z2) @ W3.T + b3
+    return out, z1, h1b, z2
+
+
+def _features(rows, seed):
+    import torch
+    from rqutils_gb300.warmstart import features_reference
+    rng = np.random.default_rng(seed)
+    s = rng.integers(0, 1 << 32, size=rows, dtype=np.uint64)
+    U = rng.uniform(2, 8, size=rows)
+    f = np.stack([features_reference(s[i:i + 1], U[i])[0] for i in range(rows)])
+    return torch.as_tensor(f).to(torch.bfloat16).cuda()
+
+
+def test_features_match_host_restatement():
+    import torch
+    from rqutils_gb300.warmstart import WarmStartMLP, features_reference
+    from rqutils_gb300 import _lib as L
+    rng = np.random.default_rng(2)
+    s = np.sort(rng.choice(1 << 32, size=1000, replace=False).astype(np.uint64))
+    x = torch.empty((1000, 64), dtype=torch.bfloat16, device='cuda')
+    st = torch.as_tensor(s.view(np.int64)).cuda()
+    L.check(L.lib().rq_mlp_features(L.ptr(st), 1000, 3.7, L.ptr(x), L.stream_ptr()), 'features')
+    ref = torch.as_tensor(features_reference(s, 3.7)).to(torch.bfloat16)
+    assert torch.equal(x.cpu(), ref)
+
+
+@pytest.mark.parametrize('rows', [128, 1000, 4096])
+def test_forward_matches_torch(rows):
+    from rqutils_gb300.warmstart import WarmStartMLP
+    m = WarmStartMLP(seed=3)
+    x = _features(rows, rows)
+    out = m.forward(x)
+    ref = _reference_forward(m, x)[0]
+    m.check_errors()
+    err = (out - ref).abs().max().item()
+    assert err < 2e-3 * max(1., ref.abs().max().item()), err
+
+
+def test_backward_matches_torch():
+    """Weight gradients of a random output gradient against the same chain rule in PyTorch
+    (BF16 operands where the kernels use them, FP32 accumulation)."""
+    import torch
+    import torch.nn.functional as F
+    from rqutils_gb300.warmstart import (OFF_B1, OFF_B2, OFF_B3, OFF_W1, OFF_W2, OFF_W3,
+                                         NPARAMS, WarmStartMLP)
+    rows = 2048
+    m = WarmStartMLP(seed=4)
+    x = _features(rows, 11)
+    out = m.forward(x)
+    g = torch.Generator().manual_seed(5)
+    dout = (torch.randn((rows, 2), generator=g) / rows).cuda()
+    m.backward(x.T.contiguous(), dout)
+    torch.cuda.synchronize()
+    m.check_errors()
+    W1, b1, W2, b2, W3, b3 = m.views()
+    _, z1, h1b, z2 = _reference_forward(m, x)
+
+    def dgelu(z):
+        return 0.5 * (1 + torch.erf(z / math.sqrt(2))) + z * torch.exp(-0.5 * z * z) / math.sqrt(2 * math.pi)
+
+    z2b = z2.to(torch.bfloat16).float()
+    dz2 = (dout @ W3) * dgelu(z2b)
+    dz2b = dz2.to(torch.bfloat16).float()
+    ref = torch.zeros(NPARAMS, dtype=torch.float32, device='cuda')
+    ref[OFF_W3:OFF_B3] = (dout.T @ F.gelu(z2b)).reshape(-1)
+    ref[OFF_B3:] = dout.sum(0)
+    ref[OFF_B2:OFF_W3] = dz2.sum(0)
+    ref[OFF_W2:OFF_B2] = (dz2b.T @ h1b).reshape(-1)
+    dz1 = (dz2b @ m.w2b.float()) * dgelu(z1.to(torch.bfloat16).float())
+    ref[OFF_B1:OFF_W2] = dz1.sum(0)
+    ref[OFF_W1:OFF_B1] = (dz1.to(torch.bfloat16).float().T @ x.float()).reshape(-1)
+    for a, b, name in [(OFF_W1, OFF_B1, 'W1'), (OFF_B1, OFF_W2, 'b1'), (OFF_W2, OFF_B2, 'W2'),
+                       (OFF_B2, OFF_W3, 'b2'), (OFF_W3, OFF_B3, 'W3'), (OFF_B3, NPARAMS, 'b3')]:
+        e = (m.grads[a:b] - ref[a:b]).norm().item() / max(ref[a:b].norm().item(), 1e-30)
+        assert e < 2e-2, (name, e)
+
+
+def test_adam_step_and_bf16_copies():
+    import torch
+    from rqutils_gb300.warmstart import NPARAMS, WarmStartMLP
+    m = WarmStartMLP(seed=6)
+    p0 = m.params.clone()
+    g = torch.randn(NPARAMS, generator=torch.Generator().manual_seed(1)).cuda()
+    m.grads.copy_(g)
+    m.step(1e-2)
+    mm = 0.1 * g
+    vv = 0.001 * g * g
+    ref = p0 - 1e-2 * (mm / 0.1) / (torch.sqrt(vv / 0.001) + 1e-8)
+    torch.cuda.synchronize()
+    assert torch.allclose(m.params, ref, rtol=1e-5, atol=1e-6)
+    W1, b1, W2, b2, W3, b3 = m.views()
+    assert torch.equal(m.w1b, W1.to(torch.bfloat16))
+    assert torch.equal(m.w2b, W2.to(torch.bfloat16))
+    assert torch.equal(m.w2tb, W2.T.contiguous().to(torch.bfloat16))
+
+
+def test_training_fits_a_smooth_family():
+    """Synthetic family psi_U(s) ~ sign(s) exp(-U w(s) / 8): the loss falls and the warm start
+    of a held-out U overlaps its target."""
+    import torch
+    from rqutils_gb300.warmstart import WarmStartMLP
+    rng = np.random.default_rng(8)
+    D = 4096
+    S = np.sort(rng.choice(1 << 20, size=D, replace=False).astype(np.uint64))
+    w = np.bitwise_count(S & np.uint64(0x3FF)).astype(np.float64)
+    sign = np.where(np.bitwise_count(S & np.uint64(0xF)) % 2 == 0, 1., -1.)
+
+    def psi_of(U):
+        v = sign * np.exp(-U * w / 8.)
+        return v / np.linalg.norm(v)
+
+    Us = np.linspace(2, 8, 16)
+    psi = torch.as_tensor(np.stack([psi_of(u) for u in Us]), dtype=torch.float32)
+    m = WarmStartMLP(seed=9)
+    losses = m.fit(S, Us, psi, steps=300, batch=8192, lr=3e-3, log_every=50)
+    assert losses[-1][1] < 0.5 * losses[0][1], losses
+    x0 = m.warm_start(S, 5.1).cpu().numpy()
+    t = psi_of(5.1)
+    assert abs(np.dot(x0, t)) / np.linalg.norm(x0) > 0.9
