@@ -148,6 +148,21 @@ int rq_terms_upload(int32_t J, int32_t K, const uint64_t *xmask, const int32_t *
  * target bucket is hash(row) ^ xhash[j]).  Setup call, stream-ordered. */
 int rq_terms_hash(const rq_terms_t *terms, uint32_t *xhash, void *stream);
 
+/* ---- sample front end ------------------------------------------------------------------ */
+
+/* Pack the reference's (rows, n) 0/1 sample rows (uint8, row stride in bytes) into uint64
+ * states, column 0 = qubit n-1 (the bit layout of sqd.py:237 without its padding bit). */
+int rq_pack_states(const uint8_t *bits, int64_t rows, int32_t n, int64_t row_stride,
+                   uint64_t *out, void *stream);
+
+/* Sort n uint64 samples and drop duplicates (uniquify_states, sqd.py:414-445, without the fill
+ * rows): out[0 .. *count) strictly increasing; `in` is left unchanged and must not alias out.
+ * Device radix sort (digits on which every sample agrees are skipped).  Synchronises the
+ * stream (the count is returned on the host). */
+int rq_uniquify_scratch_size(int64_t n, size_t *bytes);
+int rq_uniquify(const uint64_t *in, int64_t n, uint64_t *out, int64_t *count, void *scratch,
+                void *stream);
+
 /* ---- connectivity cache ---------------------------------------------------------------- */
 
 /* Pass 1 (col == NULL): fill rowptr[D+1] and return nnz.  Pass 2: fill col / grp (and val in

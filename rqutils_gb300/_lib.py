@@ -88,6 +88,11 @@ SIGNATURES = {
     'rq_xsource': (ctypes.c_int, [_P(Subspace), _c_void_p, ctypes.c_int32, _c_void_p, _c_void_p]),
     'rq_diagonal': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, _c_void_p,
                                    ctypes.c_int32, _c_void_p, _c_void_p]),
+    'rq_pack_states': (ctypes.c_int, [_c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int64,
+                                      _c_void_p, _c_void_p]),
+    'rq_uniquify_scratch_size': (ctypes.c_int, [ctypes.c_int64, _P(ctypes.c_size_t)]),
+    'rq_uniquify': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, _P(ctypes.c_int64),
+                                   _c_void_p, _c_void_p]),
     'rq_terms_upload': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _c_void_p, _c_void_p,
                                        _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
                                        _c_void_p, _c_void_p, _P(Terms), _c_void_p]),

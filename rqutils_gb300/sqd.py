@@ -9,8 +9,9 @@ tuple or a qiskit ``SparsePauliOp``; ``states`` is either the reference's (D_in,
 Pipeline (all device work in librqsqd.so):
 
 1. terms grouped by X signature and phased (``PauliSumXZ.from_paulisum(force_real=True)``);
-2. the sorted subspace with its hash table and sector filter (replaces ``uniquify_states`` and the
-   per-signature sorts of ``get_xsource``, sqd.py:414-503);
+2. the sorted subspace: sample rows packed and deduplicated by a device radix sort
+   (``uniquify_states``, sqd.py:414-445), then its hash table and sector filter (replacing the
+   per-signature sorts of ``get_xsource``, sqd.py:448-503);
 3. the operator in the mode ``cache_level`` asks for: (0, *) lookups in every matvec, (1, 0|1)
    cached source lists with diagonals recomputed (the reference default), (*, 2) cached elements;
 4. the initial vector of sqd.py:373-398 (one-hot at the first minimum of the x = 0 diagonal);
@@ -66,6 +67,53 @@ def subspace_states(states, num_qubits):
             raise ValueError('1-d uint64 states must be strictly increasing (sorted, distinct)')
         return u
     raise ValueError('states must be a (D, n) 0/1 array or a 1-d uint64 array')
+
+
+def pack_states_device(states01, device=None):
+    """(D, n) 0/1 rows -> int64 tensor of uint64 states on the device (rq_pack_states)."""
+    import ctypes  # noqa: F401  (argument types come from _lib)
+    from . import _lib as L
+    a = np.ascontiguousarray(np.asarray(states01), dtype=np.uint8)
+    rows, n = a.shape
+    if n > 64:
+        raise ValueError('at most 64 qubits are supported')
+    dev = device or default_device()
+    bits = torch.from_numpy(a).to(dev)
+    out = torch.empty(rows, dtype=torch.int64, device=dev)
+    L.check(L.lib().rq_pack_states(L.ptr(bits), rows, n, n, L.ptr(out), L.stream_ptr()),
+            'rq_pack_states')
+    return out
+
+
+def uniquify_device(packed):
+    """Sorted distinct values of a device tensor of uint64 samples (rq_uniquify)."""
+    import ctypes
+    from . import _lib as L
+    packed = packed.contiguous()
+    n = packed.numel()
+    nb = ctypes.c_size_t()
+    L.check(L.lib().rq_uniquify_scratch_size(n, ctypes.byref(nb)), 'rq_uniquify_scratch_size')
+    scratch = torch.empty(int(nb.value), dtype=torch.uint8, device=packed.device)
+    out = torch.empty_like(packed)
+    cnt = ctypes.c_int64()
+    L.check(L.lib().rq_uniquify(L.ptr(packed), n, L.ptr(out), ctypes.byref(cnt), L.ptr(scratch),
+                                L.stream_ptr()), 'rq_uniquify')
+    return out[:cnt.value]
+
+
+def subspace_states_device(states, num_qubits, device=None):
+    """Sorted distinct states on the device from either input form: (D_in, n) 0/1 rows are
+    packed and deduplicated by the device radix sort; a 1-d uint64 array is checked for strict
+    increase.  Returns (int64 device tensor, uint64 host array)."""
+    a = np.asarray(states)
+    dev = device or default_device()
+    if a.ndim == 2:
+        if a.shape[1] != num_qubits:
+            raise ValueError(f'states have {a.shape[1]} columns for {num_qubits} qubits')
+        S = uniquify_device(pack_states_device(a, dev))
+        return S, S.cpu().numpy().view(np.uint64)
+    u = subspace_states(a, num_qubits)
+    return torch.from_numpy(u.view(np.int64)).to(dev), u
 
 
 def cache_mode(cache_level):
@@ -124,9 +172,9 @@ def sqd(hamiltonian, states, states_size=None, return_eigvec=True, cache_level=(
         raise ValueError('states_size smaller than the states array length')
     if not isinstance(hamiltonian, PauliSumXZ):
         hamiltonian = PauliSumXZ.from_paulisum(hamiltonian, force_real=True, add_padding=True)
-    S = subspace_states(states, hamiltonian.num_qubits)
     start = time.time()
-    prob = SQDProblem(hamiltonian, S, cache_level=cache_level, lookup=lookup, device=device,
+    S_dev, S = subspace_states_device(states, hamiltonian.num_qubits, device)
+    prob = SQDProblem(hamiltonian, S_dev, cache_level=cache_level, lookup=lookup, device=device,
                       precision=precision)
     x0 = prob.initial_vector()
     eig, x, info = lobpcg_solve(prob.op, x0, maxiter=maxiter, tol=tol, tol_dim=states_size,

@@ -176,3 +176,87 @@ def features_reference(states, U):
     u = np.broadcast_to(u, (len(s),))
     f[:, 32], f[:, 33], f[:, 34] = u, u * u, u * u * u
     return f
+
+
+# ---------------------------------------------------------------------------------------------
+# Hubbard family: training data and evaluation of start vectors
+# ---------------------------------------------------------------------------------------------
+def _hubbard_operator(sub, U, Lx, Ly, t, periodic, device):
+    from .device import DeviceOperator, DeviceTerms
+    from .paulis.symplectic import PauliSumXZ
+    from .workloads import hubbard_jw
+    ham = PauliSumXZ.from_paulisum(hubbard_jw(Lx, Ly, t, float(U), periodic), force_real=True,
+                                   add_padding=True)
+    return DeviceOperator(DeviceTerms(ham, device=device), sub, mode='conn')
+
+
+def hubbard_family(S, Us, Lx=4, Ly=4, t=1.0, periodic=True, target_rel=1e-7, maxiter=5000,
+                   seed=0, device=None):
+    """Ground states of the Hubbard models at every U on the sorted subspace S, solved by the
+    plain LOBPCG solver with continuation: U ascending, each solve started from the previous
+    ground state (the first from a seeded random vector).  Signs are aligned with the previous
+    state (the first has its largest component positive).  Returns (psi (P, D) FP32 in the
+    order of Us, eigenvalues, iterations)."""
+    from .device import DeviceSubspace
+    from .ground_locg import lobpcg_solve
+    dev = device or default_device()
+    sub = DeviceSubspace(S, num_qubits=2 * Lx * Ly, device=dev)
+    Us = np.asarray(Us, dtype=np.float64)
+    psi = torch.empty((len(Us), sub.D), dtype=torch.float32, device=dev)
+    eig = np.zeros(len(Us))
+    its = np.zeros(len(Us), dtype=np.int64)
+    x = torch.as_tensor(np.random.default_rng(seed).normal(size=sub.D), device=dev)
+    prev = None
+    for i in np.argsort(Us, kind='stable'):
+        op = _hubbard_operator(sub, Us[i], Lx, Ly, t, periodic, dev)
+        e, x, info = lobpcg_solve(op, x, maxiter=maxiter, target_rel=target_rel, variant='fast')
+        if prev is None:
+            if x[int(torch.argmax(x.abs()))] < 0:
+                x = -x
+        elif torch.dot(x, prev) < 0:
+            x = -x
+        prev = x
+        psi[i] = x.float()
+        eig[i] = e
+        its[i] = info['niter']
+    return psi, eig, its
+
+
+def evaluate_starts(model, S, Us, Lx=4, Ly=4, t=1.0, periodic=True, target_rel=1e-8,
+                    maxiter=5000, seed=0, device=None, mixed=True, variant='fast'):
+    """LOBPCG to |r| <= target_rel |theta| on each U from three start vectors: the network's
+    ('learned', inference included in the time), a seeded random vector ('random') and the
+    reference's one-hot at the lowest diagonal entry ('reference').  Returns {start: [dict]}."""
+    import time
+    from .device import DeviceSubspace
+    from .ground_locg import lobpcg_solve
+    dev = device or default_device()
+    sub = DeviceSubspace(S, num_qubits=2 * Lx * Ly, device=dev)
+    rng = np.random.default_rng(seed)
+    res = {'learned': [], 'random': [], 'reference': []}
+    for U in np.asarray(Us, dtype=np.float64):
+        op = _hubbard_operator(sub, U, Lx, Ly, t, periodic, dev)
+        xr = torch.as_tensor(rng.normal(size=sub.D), device=dev)
+        for name in res:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if name == 'learned':
+                x0 = model.warm_start(sub.states, U, torch.float64)
+            elif name == 'random':
+                x0 = xr
+            else:
+                x0 = torch.zeros(sub.D, dtype=torch.float64, device=dev)
+                x0[int(torch.argmin(op.diag0))] = 1.
+            e, x, info = lobpcg_solve(op, x0, maxiter=maxiter, target_rel=target_rel,
+                                      variant=variant, mixed=mixed)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            ax = op.matvec(x)
+            rel = float(torch.linalg.vector_norm(ax - e * x) / abs(e))
+            ov = None
+            if name == 'learned':
+                ov = float(abs(torch.dot(x0, x)) / torch.linalg.vector_norm(x0))
+            res[name].append({'U': float(U), 'iterations': info['niter'], 'time_s': dt,
+                              'eigval': e, 'rel_residual': rel, 'converged': info['converged'],
+                              'start_overlap': ov})
+    return res

@@ -181,3 +181,30 @@ def test_training_fits_a_smooth_family():
     x0 = m.warm_start(S, 5.1).cpu().numpy()
     t = psi_of(5.1)
     assert abs(np.dot(x0, t)) / np.linalg.norm(x0) > 0.9
+
+
+def test_hubbard_family_and_learned_start_small():
+    """Hubbard 4x2 family on a low-double-occupancy subspace: continuation ground states match
+    dense diagonalisation; a network trained on 24 values of U starts held-out solves close to
+    their ground states, and they converge to the same energies as from random starts."""
+    import torch
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    from rqutils_gb300.sqd import hproj
+    from rqutils_gb300.warmstart import WarmStartMLP, evaluate_starts, hubbard_family
+    from rqutils_gb300.workloads import hubbard_jw, low_double_occupancy_states
+    rng = np.random.default_rng(12)
+    S = low_double_occupancy_states(rng, 1000, Ns=8)
+    Us = np.linspace(2., 8., 24)
+    psi, eig, its = hubbard_family(S, Us, Lx=4, Ly=2)
+    for k in (0, 11, 23):
+        h = PauliSumXZ.from_paulisum(hubbard_jw(4, 2, 1.0, Us[k]), force_real=True, add_padding=True)
+        e_dense = np.linalg.eigvalsh(hproj(h, S).toarray())[0]
+        assert abs(eig[k] - e_dense) <= 1e-6 * abs(e_dense), (k, eig[k], e_dense)
+    m = WarmStartMLP(seed=1)
+    m.fit(S, Us, psi, steps=400, batch=4096, lr=3e-3)
+    res = evaluate_starts(m, S, [3.3, 6.1], Lx=4, Ly=2)
+    for rl, rr in zip(res['learned'], res['random']):
+        assert rl['converged'] and rr['converged']
+        assert rl['start_overlap'] > 0.8, rl
+        assert abs(rl['eigval'] - rr['eigval']) <= 1e-9 * abs(rr['eigval'])
+        assert rl['rel_residual'] < 1e-7
