@@ -592,13 +592,59 @@ def run_profile(args):
     import torch
     from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
     dev = torch.device('cuda', torch.cuda.current_device())
+    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    if args.workload == 'batched':
+        from rqutils_gb300.batch import BatchedSQD
+        wl = BatchWorkload()
+        b = BatchedSQD(wl.hams, wl.S, cache_level=(0, 0), device=dev)
+        x = torch.as_tensor(wl.x).to(dev, torch.complex64)
+        y = torch.empty_like(x)
+        for _ in range(args.warmup):
+            b.matvec(x, out=y)
+        times = time_steps(lambda: b.matvec(x, out=y), args.steps, lambda: flush_buf.fill_(1.0),
+                           torch.cuda.current_stream())
+        b.check_errors()
+        print(json.dumps({'profile_steps': args.steps, 'ms': times}), flush=True)
+        return
+    if args.workload == 'warmstart':
+        # training steps of the warm-start network (tcgen05 GEMMs) on 65,536-row batches
+        from rqutils_gb300.warmstart import WarmStartMLP
+        rng = np.random.default_rng(0)
+        D = 1 << 16
+        S = np.sort(rng.choice(1 << 32, size=D, replace=False).astype(np.uint64))
+        psi = torch.as_tensor(rng.normal(size=(8, D)), dtype=torch.float32)
+        psi /= torch.linalg.vector_norm(psi, dim=1, keepdim=True)
+        m = WarmStartMLP(device=dev)
+        m.fit(S, np.linspace(2, 8, 8), psi, steps=args.warmup, batch=65536)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.fit(S, np.linspace(2, 8, 8), psi, steps=args.steps, batch=65536)
+        torch.cuda.synchronize()
+        print(json.dumps({'profile_steps': args.steps,
+                          'ms_per_step': 1e3 * (time.perf_counter() - t0) / args.steps}), flush=True)
+        return
     wl = Workload(args.workload, args.rows)
     terms = DeviceTerms(wl.ham, device=dev)
     sub = DeviceSubspace(wl.S, num_qubits=wl.nq, device=dev)
+    if args.lobpcg:
+        # LOBPCG solves (cached connectivity, FAST variant, mixed precision, 64 iterations) from a
+        # seeded random start: the launch list of the solver
+        from rqutils_gb300.ground_locg import lobpcg_solve
+        op = DeviceOperator(terms, sub, mode='conn')
+        rng = np.random.default_rng(0)
+        xr = torch.as_tensor(rng.normal(size=sub.D) + 1j * rng.normal(size=sub.D), device=dev)
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lobpcg_solve(op, xr.clone(), maxiter=64, tol=1e-300, variant='fast', mixed=True)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                print(json.dumps({'lobpcg_64_iterations_ms': 1e3 * (time.perf_counter() - t0)}),
+                      flush=True)
+        return
     op = DeviceOperator(terms, sub, mode='free')
     x = torch.as_tensor(wl.x).to(dev, torch.complex64 if wl.vtype == 'c64' else torch.complex128)
     y = torch.empty_like(x)
-    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
         op.matvec(x, out=y)
     times = time_steps(lambda: op.matvec(x, out=y), args.steps,
@@ -741,6 +787,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--profile', action='store_true',
                     help='run only the timed matvec loop (for ncu captures)')
+    ap.add_argument('--lobpcg', action='store_true',
+                    help='with --profile: run LOBPCG solves instead of the matvec loop')
     ap.add_argument('--no-warmstart', action='store_true',
                     help='skip the learned-warm-start study of the hubbard workload')
     ap.add_argument('--rows', type=int, default=None,
