@@ -77,11 +77,14 @@ typedef struct rq_subspace {
     int32_t   hbits;         /* log2(number of buckets), from rq_subspace_sizes            */
     int32_t   lookup;        /* RQ_LOOKUP_*                                                */
     int32_t   key_bits;      /* 32: states and every X mask < 2^32 (16-byte buckets); 64   */
-    int32_t   pad_;
+    int32_t   pbits;         /* presence bitmap size log2 (rq_presence_bits), 0 = none     */
     uint64_t  empty_key;     /* written by rq_subspace_build: a value not in states        */
     uint64_t  fmask_a;       /* sector filter masks (0, 0 = filter off)                    */
     uint64_t  fmask_b;
     uint32_t *fbits;         /* [RQ_FILTER_WORDS], written by rq_subspace_build            */
+    uint32_t *pmap;          /* [2^pbits / 32]: bit (hash(s) >> (32 - pbits)) set for every
+                                state, written by rq_subspace_build; a lookup whose bit is
+                                clear skips the table (NULL = none)                        */
 } rq_subspace_t;
 
 typedef struct rq_terms {
@@ -115,6 +118,11 @@ typedef struct rq_operator {
 /* Hash-table bucket count exponent for D states at load factor <= 1/8 (4 keys per bucket):
  * hkeys takes (key_bits / 2) << hbits bytes, hvals 4 << hbits int32. */
 int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits);
+
+/* Presence bitmap size for D states: 0 when the hash table is small enough to stay in L2
+ * (<= 64 MB), else pbits = min(29, hbits + 2) (at most 64 MB of bitmap, a bit set for ~1/8 of
+ * the misses).  The bitmap takes 2^pbits / 8 bytes. */
+int rq_presence_bits(int64_t D, int32_t key_bits, int32_t *pbits);
 
 /* Bytes of scratch that rq_matvec / rq_conn_build / rq_dots need for their reductions/scans. */
 int rq_scratch_size(int64_t D, size_t *bytes);
@@ -195,7 +203,9 @@ typedef struct rq_lobpcg_params {
     double  switch_rel;     /* mixed: leave the 32-bit phase when |r| < switch_rel * |theta|  */
     double  target_rel;     /* > 0: also stop when |r| <= target_rel * |theta| (FP64 residual) */
     int32_t refresh;        /* FAST: recompute A x, A y every `refresh` iterations (0 = 32)  */
-    int32_t use_graph;      /* 1: run the loop as one CUDA graph with a device-side while    */
+    int32_t use_graph;      /* 0: eager launches; 1: one persistent cooperative kernel per
+                               precision phase for RQ_MODE_CONN / RQ_MODE_CSR operators, CUDA
+                               graphs of 8 iterations otherwise; 2: CUDA graphs only        */
     int32_t jacobi;         /* 1: precondition the residual with (diag(H) - theta)^-1        */
     int32_t guard;          /* 1: where the reference arithmetic gives 0/0 (a degenerate
                                Cardano eigenvector, |s| = 0) take a finite replacement; only
@@ -260,7 +270,7 @@ typedef struct rq_batch {
     void    *hkeys;            /* hash table over the composite keys: 32 << hbits bytes          */
     int32_t *hvals;            /* [4 << hbits]                                                   */
     int32_t  hbits;            /* rq_subspace_sizes(D, 64, &hbits)                               */
-    int32_t  pad_;
+    int32_t  pbits;            /* rq_presence_bits(D, 64, &pbits); 0 = no presence bitmap        */
     uint64_t empty_key;        /* written by rq_batch_build                                      */
     const uint64_t *fmask;     /* [2P] sector filter masks (a, b) of each problem; NULL = off    */
     uint32_t *fbits;           /* [P * RQ_FILTER_WORDS], written by rq_batch_build               */
@@ -274,6 +284,7 @@ typedef struct rq_batch {
     int64_t  nnz;
     const int64_t *states_size; /* [P] HOST array: each problem's convergence length (sqd's
                                    states_size, sqd.py:222-225); NULL = its row count        */
+    uint32_t *pmap;            /* [2^pbits / 32] presence bitmap over the composite keys       */
 } rq_batch_t;
 
 /* Validate the keys, fill the hash table, the per-problem sector filters and diag0.
@@ -354,6 +365,17 @@ int rq_mlp_warm_start(int64_t D, const float *out, int32_t vtype, void *x0, void
  * (error flag). */
 int rq_bf16_gemm(const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb, int64_t M,
                  int32_t N, int64_t K, float *C, void *ws, void *stream);
+
+/* ---- state-vector simulation ------------------------------------------------------------- */
+
+/* Apply Pauli-rotation gates in order to a complex128 state of 2^n amplitudes, in place (the
+ * reference's svsim, svsim.py:88-122): gate g maps
+ *     out[i] = i sin[g] (-1)^popcount(i & z[g]) state[i ^ x[g]] + cos[g] state[i]
+ * (the cos term is omitted when cos[g] == 0).  x, z, cos, sin are HOST arrays of ngates
+ * entries (the gate list of CircuitXZ, svsim.py:42-49); gates_scratch is device memory of
+ * 32 * ngates bytes.  Synchronises the stream. */
+int rq_svsim(const uint64_t *x, const uint64_t *z, const double *cos_, const double *sin_,
+             int32_t ngates, int32_t n, void *state, void *gates_scratch, void *stream);
 
 /* ---- diagnostics ------------------------------------------------------------------------- */
 

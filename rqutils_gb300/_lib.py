@@ -24,9 +24,9 @@ _c_void_p = ctypes.c_void_p
 class Subspace(ctypes.Structure):
     _fields_ = [('states', _c_void_p), ('D', ctypes.c_int64), ('hkeys', _c_void_p),
                 ('hvals', _c_void_p), ('hbits', ctypes.c_int32), ('lookup', ctypes.c_int32),
-                ('key_bits', ctypes.c_int32), ('pad_', ctypes.c_int32),
+                ('key_bits', ctypes.c_int32), ('pbits', ctypes.c_int32),
                 ('empty_key', ctypes.c_uint64), ('fmask_a', ctypes.c_uint64),
-                ('fmask_b', ctypes.c_uint64), ('fbits', _c_void_p)]
+                ('fmask_b', ctypes.c_uint64), ('fbits', _c_void_p), ('pmap', _c_void_p)]
 
 
 class Terms(ctypes.Structure):
@@ -62,11 +62,11 @@ class LobpcgResult(ctypes.Structure):
 class Batch(ctypes.Structure):
     _fields_ = [('P', ctypes.c_int32), ('mode', ctypes.c_int32), ('keys', _c_void_p),
                 ('prow', _c_void_p), ('D', ctypes.c_int64), ('hkeys', _c_void_p),
-                ('hvals', _c_void_p), ('hbits', ctypes.c_int32), ('pad_', ctypes.c_int32),
+                ('hvals', _c_void_p), ('hbits', ctypes.c_int32), ('pbits', ctypes.c_int32),
                 ('empty_key', ctypes.c_uint64), ('fmask', _c_void_p), ('fbits', _c_void_p),
                 ('terms', Terms), ('gofs', _c_void_p), ('dgrp', _c_void_p), ('diag0', _c_void_p),
                 ('rowptr', _c_void_p), ('col', _c_void_p), ('grp', _c_void_p),
-                ('nnz', ctypes.c_int64), ('states_size', _c_void_p)]
+                ('nnz', ctypes.c_int64), ('states_size', _c_void_p), ('pmap', _c_void_p)]
 
 
 BATCH_STATE_BITS = 40
@@ -83,6 +83,7 @@ class Mlp(ctypes.Structure):
 _P = ctypes.POINTER
 SIGNATURES = {
     'rq_subspace_sizes': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int32)]),
+    'rq_presence_bits': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int32)]),
     'rq_scratch_size': (ctypes.c_int, [ctypes.c_int64, _P(ctypes.c_size_t)]),
     'rq_subspace_build': (ctypes.c_int, [_P(Subspace), _c_void_p, _c_void_p]),
     'rq_xsource': (ctypes.c_int, [_P(Subspace), _c_void_p, ctypes.c_int32, _c_void_p, _c_void_p]),
@@ -141,6 +142,8 @@ SIGNATURES = {
     'rq_bf16_gemm': (ctypes.c_int, [_c_void_p, ctypes.c_int64, _c_void_p, ctypes.c_int64,
                                     ctypes.c_int64, ctypes.c_int32, ctypes.c_int64, _c_void_p,
                                     _c_void_p, _c_void_p]),
+    'rq_svsim': (ctypes.c_int, [_c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int32,
+                                ctypes.c_int32, _c_void_p, _c_void_p, _c_void_p]),
     'rq_last_error': (ctypes.c_char_p, []),
     'rq_version': (ctypes.c_int, []),
 }

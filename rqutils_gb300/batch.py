@@ -81,7 +81,7 @@ class BatchedSQD:
     """
 
     def __init__(self, hamiltonians, states_list, cache_level=(0, 0), states_sizes=None,
-                 filter=True, device=None, stream=None):
+                 filter=True, device=None, stream=None, presence=None):
         if len(hamiltonians) != len(states_list) or not hamiltonians:
             raise ValueError('need one subspace per Hamiltonian and at least one problem')
         self.device = device or default_device()
@@ -135,6 +135,11 @@ class BatchedSQD:
         L.check(lib.rq_subspace_sizes(self.D, 64, ctypes.byref(hb)), 'rq_subspace_sizes')
         self.hkeys = torch.empty(4 << hb.value, dtype=torch.int64, device=dev)
         self.hvals = torch.empty(4 << hb.value, dtype=torch.int32, device=dev)
+        pb = ctypes.c_int32()
+        L.check(lib.rq_presence_bits(self.D, 64, ctypes.byref(pb)), 'rq_presence_bits')
+        self.pbits = pb.value if presence is None else (0 if presence is False else int(presence))
+        self.pmap = (torch.empty((1 << self.pbits) // 32, dtype=torch.int32, device=dev)
+                     if self.pbits else None)
         if filter:
             fm = np.array([default_filter_masks(h.num_qubits) for h in hams],
                           dtype=np.uint64).reshape(-1)
@@ -146,10 +151,11 @@ class BatchedSQD:
         self.scratch = scratch_tensor(self.D, dev)
         self.c = L.Batch(P=self.P, mode=L.MODE_FREE, keys=L.ptr(self.keys),
                          prow=L.ptr(self.prow_t), D=self.D, hkeys=L.ptr(self.hkeys),
-                         hvals=L.ptr(self.hvals), hbits=hb.value, empty_key=0,
+                         hvals=L.ptr(self.hvals), hbits=hb.value, pbits=self.pbits, empty_key=0,
                          fmask=L.ptr(self.fmask), fbits=L.ptr(self.fbits), terms=terms,
                          gofs=L.ptr(self.gofs), dgrp=L.ptr(self.dgrp), diag0=L.ptr(self.diag0),
-                         states_size=ctypes.cast(self.states_size, ctypes.c_void_p))
+                         states_size=ctypes.cast(self.states_size, ctypes.c_void_p),
+                         pmap=L.ptr(self.pmap))
         L.check(lib.rq_batch_build(ctypes.byref(self.c), L.ptr(self.scratch), L.stream_ptr(stream)),
                 'rq_batch_build')
         self.rowptr = self.col = self.grp = None

@@ -14,7 +14,7 @@ namespace rq {
 
 int build_key_table(const uint64_t *keys, int64_t D, int key_bits, bool hash, void *hkeys,
                     int32_t *hvals, int hbits, uint64_t *empty_out, int *flag,
-                    unsigned long long *gap, cudaStream_t st);
+                    unsigned long long *gap, cudaStream_t st, uint32_t *pmap, int pbits);
 
 namespace {
 
@@ -145,11 +145,22 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
                 const uint64_t ts = s ^ xv;
                 q[u] = in && (t[u] != B.empty_key) &&
                        (!B.fmask || sector_ok(fb, fa, fbm, ts));
-                b[u] = (hs ^ hx) >> shift;
+                b[u] = hs ^ hx;
+            }
+            if (B.pbits > 0) {
+                uint32_t pw[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t idx = b[u] >> (32 - B.pbits);
+                    pw[u] = q[u] ? __ldg(B.pmap + (idx >> 5)) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    q[u] = q[u] && ((pw[u] >> ((b[u] >> (32 - B.pbits)) & 31)) & 1u);
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                w[u] = KeyWidth<64>::load(keys + (size_t)b[u] * 32, q[u], B.empty_key);
+                w[u] = KeyWidth<64>::load(keys + (size_t)(b[u] >> shift) * 32, q[u], B.empty_key);
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 bool any, open;
@@ -331,8 +342,10 @@ RQ_API int rq_batch_build(rq_batch_t *b, void *scratch, void *stream) {
     }
     int *flag = scratch_err(scratch);
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
+    if (b->pbits != 0 && (!b->pmap || b->pbits < 5 || b->pbits > 32 || b->pbits < b->hbits))
+        return fail(RQ_E_ARG, "rq_batch_build: presence bitmap missing or pbits out of range");
     int rc = build_key_table(b->keys, b->D, 64, true, b->hkeys, b->hvals, b->hbits, &b->empty_key,
-                             flag, gap, st);
+                             flag, gap, st, b->pbits ? b->pmap : nullptr, b->pbits);
     if (rc != RQ_OK) return fail(rc, std::string("rq_batch_build: ") + rq_last_error());
     RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     k_batch_check_rows<<<grid_rows(b->D), kThreads, 0, st>>>(b->keys, b->D, b->prow, b->P, flag);

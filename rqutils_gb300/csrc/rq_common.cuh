@@ -160,6 +160,12 @@ __device__ __forceinline__ uint32_t bucket_from_hash(uint32_t h, int hbits) {
     return h >> (32 - hbits);
 }
 
+// presence bitmap test: bit (h >> (32 - pbits)) of pmap
+__device__ __forceinline__ bool present(const uint32_t *pmap, uint32_t h, int pbits) {
+    const uint32_t idx = h >> (32 - pbits);
+    return (__ldg(pmap + (idx >> 5)) >> (idx & 31)) & 1u;
+}
+
 template <int KB>
 struct KeyWidth;
 template <>
@@ -289,43 +295,91 @@ __device__ __forceinline__ bool sector_ok_k(const uint32_t *fb, K a, K b, K t) {
 }
 
 // ------------------------------------------------------------------------------------------
-// deterministic grid reduction of NV complex doubles
+// double-float sums: GB300 issues FP64 at a small fraction of its FP32 rate, so reduction trees
+// (shuffles, shared memory, the last block's pass over the partials) add pairs of floats
+// (hi + lo, ~48-bit significand) instead of doubles
 // ------------------------------------------------------------------------------------------
-// Scratch layout: [counter (uint32, 16 B slot)] [partials: gridDim.x * NV double2].
-// Each block writes its partials; the last block to finish sums them in block order and writes
-// `out`, then resets the counter so the scratch can be reused by the next launch.
+struct df {
+    float hi, lo;
+};
+struct cdf {
+    df re, im;
+};
+
+__device__ __forceinline__ df df_of(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_val(df a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ df df_add(df a, df b) {
+    float s, e, t, f;
+    two_sum(a.hi, b.hi, s, e);
+    two_sum(a.lo, b.lo, t, f);
+    e += t;
+    float h = s + e;
+    e = e - (h - s);
+    e += f;
+    s = h + e;
+    e = e - (s - h);
+    return {s, e};
+}
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
+__device__ __forceinline__ cdf cdf_of(double2 v) { return {df_of(v.x), df_of(v.y)}; }
+__device__ __forceinline__ double2 cdf_val(cdf a) { return make_double2(df_val(a.re), df_val(a.im)); }
+__device__ __forceinline__ cdf cdf_shfl_xor(cdf a, int o) {
+    return {{__shfl_xor_sync(0xffffffffu, a.re.hi, o), __shfl_xor_sync(0xffffffffu, a.re.lo, o)},
+            {__shfl_xor_sync(0xffffffffu, a.im.hi, o), __shfl_xor_sync(0xffffffffu, a.im.lo, o)}};
+}
+__device__ __forceinline__ cdf cdf_zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+__device__ __forceinline__ float4 cdf_pack(cdf a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
+__device__ __forceinline__ cdf cdf_unpack(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
+
+// Block-wide sum of NV values (every thread passes its own); the result is valid in warp 0,
+// lane 0.  `red` is shared scratch of [warps][NV].
 template <int NV>
-__device__ void grid_reduce(double2 (&v)[NV], void *scratch, double2 *out) {
-    __shared__ double2 red[kThreads / 32][NV];
-    __shared__ bool last;
-    unsigned int *counter = reinterpret_cast<unsigned int *>(scratch);
-    double2 *part = reinterpret_cast<double2 *>(reinterpret_cast<char *>(scratch) + 16);
+__device__ __forceinline__ void block_sum(cdf (&w)[NV], cdf (*red)[NV]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarp = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            v[k].x += __shfl_xor_sync(0xffffffffu, v[k].x, o);
-            v[k].y += __shfl_xor_sync(0xffffffffu, v[k].y, o);
-        }
-        if (lane == 0) red[warp][k] = v[k];
+        for (int o = 16; o > 0; o >>= 1) w[k] = cdf_add(w[k], cdf_shfl_xor(w[k], o));
+        if (lane == 0) red[warp][k] = w[k];
     }
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            double2 a = (lane < nwarp) ? red[lane][k] : make_double2(0., 0.);
+            w[k] = (lane < nwarp) ? red[lane][k] : cdf_zero();
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-                a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-            }
-            if (lane == 0) part[(size_t)blockIdx.x * NV + k] = a;
+            for (int o = 16; o > 0; o >>= 1) w[k] = cdf_add(w[k], cdf_shfl_xor(w[k], o));
         }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// deterministic grid reduction of NV complex values
+// ------------------------------------------------------------------------------------------
+// Scratch layout: [counter (uint32, 16 B slot)] [partials: gridDim.x * NV double-float pairs].
+// Each block writes its partials; the last block to finish sums them in block order and writes
+// `out`, then resets the counter so the scratch can be reused by the next launch.
+template <int NV>
+__device__ void grid_reduce(cdf (&v)[NV], void *scratch, double2 *out) {
+    __shared__ cdf red[kThreads / 32][NV];
+    __shared__ bool last;
+    unsigned int *counter = reinterpret_cast<unsigned int *>(scratch);
+    float4 *part = reinterpret_cast<float4 *>(reinterpret_cast<char *>(scratch) + 16);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    cdf w[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) w[k] = v[k];
+    block_sum<NV>(w, red);
+    if (warp == 0) {
         if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) part[(size_t)blockIdx.x * NV + k] = cdf_pack(w[k]);
             __threadfence();
-            unsigned int t = atomicAdd(counter, 1u);
+            const unsigned int t = atomicAdd(counter, 1u);
             last = (t == gridDim.x - 1);
         }
     }
@@ -334,37 +388,17 @@ __device__ void grid_reduce(double2 (&v)[NV], void *scratch, double2 *out) {
     __threadfence();
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        double2 a = make_double2(0., 0.);
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-            double2 p = __ldcg(part + (size_t)b * NV + k);
-            a.x += p.x;
-            a.y += p.y;
-        }
-        v[k] = a;
+        cdf a = cdf_zero();
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            a = cdf_add(a, cdf_unpack(__ldcg(part + (size_t)b * NV + k)));
+        w[k] = a;
     }
     __syncthreads();  // red[] reuse
+    block_sum<NV>(w, red);
+    if (warp == 0 && lane == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            v[k].x += __shfl_xor_sync(0xffffffffu, v[k].x, o);
-            v[k].y += __shfl_xor_sync(0xffffffffu, v[k].y, o);
-        }
-        if (lane == 0) red[warp][k] = v[k];
-    }
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double2 a = (lane < nwarp) ? red[lane][k] : make_double2(0., 0.);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-                a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-            }
-            if (lane == 0) out[k] = a;
-        }
-        if (lane == 0) *counter = 0u;
+        for (int k = 0; k < NV; ++k) out[k] = cdf_val(w[k]);
+        *counter = 0u;
     }
 }
 

@@ -24,6 +24,7 @@
 
 #include "rq_common.cuh"
 #include "rq_host.h"
+#include "rq_rows.cuh"
 
 namespace rq {
 
@@ -81,6 +82,11 @@ struct DotAcc<float> {
     }
     __device__ __forceinline__ void nprod(float a, float b) { prod(-a, b); }
     __device__ __forceinline__ double get() const { return (double)s + (double)c; }
+    // the same sum as a double-float, without FP64 arithmetic
+    __device__ __forceinline__ df get_df() const {
+        const float h = s + c;
+        return {h, c - (h - s)};
+    }
 };
 
 template <>
@@ -89,6 +95,7 @@ struct DotAcc<double> {
     __device__ __forceinline__ void prod(double a, double b) { s = fma(a, b, s); }
     __device__ __forceinline__ void nprod(double a, double b) { s = fma(-a, b, s); }
     __device__ __forceinline__ double get() const { return s; }
+    __device__ __forceinline__ df get_df() const { return df_of(s); }
 };
 
 template <typename R>
@@ -104,6 +111,7 @@ struct CDot {
         }
     }
     __device__ __forceinline__ double2 get() const { return make_double2(re.get(), im.get()); }
+    __device__ __forceinline__ cdf get_cdf() const { return {re.get_df(), im.get_df()}; }
 };
 
 template <typename R>
@@ -126,6 +134,14 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 // segment policies: which rows a block handles and where its sums go
 // ------------------------------------------------------------------------------------------
 
+// Grid barrier of the persistent LOBPCG kernel (zeroed before each launch).
+struct GridBar {
+    unsigned int count;
+    unsigned int gen;
+    int abort;
+    int pad_;
+};
+
 // One problem: grid-stride over [0, D), deterministic grid reduction into the state.
 struct SegOne {
     State *st;
@@ -138,7 +154,7 @@ struct SegOne {
     __device__ __forceinline__ int64_t end() const { return D; }
     __device__ __forceinline__ int64_t stride() const { return (int64_t)gridDim.x * blockDim.x; }
     template <int NV>
-    __device__ void reduce(double2 (&v)[NV], int slot) const {
+    __device__ void reduce(cdf (&v)[NV], int slot) const {
         grid_reduce<NV>(v, red, st->red + slot);
     }
 };
@@ -158,54 +174,46 @@ struct SegBatch {
     __device__ __forceinline__ int64_t end() const { return crow[blockIdx.x + 1]; }
     __device__ __forceinline__ int64_t stride() const { return blockDim.x; }
     template <int NV>
-    __device__ void reduce(double2 (&v)[NV], int slot) const {
-        __shared__ double2 red[kThreads / 32][NV];
+    __device__ void reduce(cdf (&v)[NV], int slot) const {
+        __shared__ cdf red[kThreads / 32][NV];
         __shared__ bool last;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        const int nwarp = (blockDim.x + 31) >> 5;
         const int c = blockIdx.x, p = cprob[c];
+        float4 *pt = reinterpret_cast<float4 *>(part);
+        cdf w[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
+        for (int k = 0; k < NV; ++k) w[k] = v[k];
+        block_sum<NV>(w, red);
+        if (warp == 0 && lane == 0) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                v[k].x += __shfl_xor_sync(0xffffffffu, v[k].x, o);
-                v[k].y += __shfl_xor_sync(0xffffffffu, v[k].y, o);
-            }
-            if (lane == 0) red[warp][k] = v[k];
-        }
-        __syncthreads();
-        if (warp == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                double2 a = (lane < nwarp) ? red[lane][k] : make_double2(0., 0.);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-                    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-                }
-                if (lane == 0) part[(size_t)c * kMaxReduce + k] = a;
-            }
-            if (lane == 0) {
-                __threadfence();
-                const unsigned int n = (unsigned int)(cofs[p + 1] - cofs[p]);
-                last = (atomicAdd(counter + p, 1u) == n - 1);
-            }
+            for (int k = 0; k < NV; ++k) pt[(size_t)c * kMaxReduce + k] = cdf_pack(w[k]);
+            __threadfence();
+            const unsigned int n = (unsigned int)(cofs[p + 1] - cofs[p]);
+            last = (atomicAdd(counter + p, 1u) == n - 1);
         }
         __syncthreads();
         if (!last) return;
         __threadfence();
         if (threadIdx.x < NV) {  // chunk order: deterministic
-            double2 a = make_double2(0., 0.);
-            for (int cc = cofs[p]; cc < cofs[p + 1]; ++cc) {
-                const double2 q = __ldcg(part + (size_t)cc * kMaxReduce + threadIdx.x);
-                a.x += q.x;
-                a.y += q.y;
-            }
-            states[p].red[slot + threadIdx.x] = a;
+            cdf a = cdf_zero();
+            for (int cc = cofs[p]; cc < cofs[p + 1]; ++cc)
+                a = cdf_add(a, cdf_unpack(__ldcg(pt + (size_t)cc * kMaxReduce + threadIdx.x)));
+            states[p].red[slot + threadIdx.x] = cdf_val(a);
         }
         if (threadIdx.x == 0) counter[p] = 0u;
     }
 };
+
+// Scalars that every thread of a block needs (square roots, quotients of the reduced sums) are
+// computed once by thread 0 and shared: GB300 runs FP64 division and square roots at a small
+// fraction of its FP32 rate, so per-thread copies cost more than the pass itself at D <= 2^20.
+#define BLOCK_SCALARS(n, body)        \
+    __shared__ double bs_[n];         \
+    if (threadIdx.x == 0) {           \
+        double *out = bs_;            \
+        body;                         \
+    }                                 \
+    __syncthreads();
 
 #define SEG_LOOP(i) for (int64_t i = seg.begin(); i < seg.end(); i += seg.stride())
 
@@ -221,8 +229,7 @@ struct Pairs {
 };
 
 template <typename V, int NP, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_dots(SEG seg, Pairs<V, NP> pr, int slot) {
+__device__ __forceinline__ void d_dots(SEG seg, Pairs<V, NP> pr, int slot) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -232,31 +239,42 @@ k_dots(SEG seg, Pairs<V, NP> pr, int slot) {
         for (int k = 0; k < NP; ++k)
             acc[k].add(VT<V>::ld(pr.a[k], i), VT<V>::ld(pr.b[k], i), VT<V>::kComplex);
     }
-    double2 v[NP];
+    cdf v[NP];
 #pragma unroll
-    for (int k = 0; k < NP; ++k) v[k] = acc[k].get();
+    for (int k = 0; k < NP; ++k) v[k] = acc[k].get_cdf();
     seg.template reduce<NP>(v, slot);
+}
+template <typename V, int NP, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_dots(SEG seg, Pairs<V, NP> pr, int slot) {
+    d_dots<V, NP, SEG>(seg, pr, slot);
 }
 
 // out = v * scale where scale = 1 / sqrt(red[nslot].x) (1 when that is 0); optional <x,out>, <y,out>
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_normalize(SEG seg, const V *in, V *out, int nslot) {
+__device__ __forceinline__ void d_normalize(SEG seg, const V *in, V *out, int nslot) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const double n = sqrt(st->red[nslot].x);
-    const R inv = (R)(n == 0. ? 1. : 1. / n);
+    BLOCK_SCALARS(1, {
+        const double n = sqrt(st->red[nslot].x);
+        out[0] = n == 0. ? 1. : 1. / n;
+    })
+    const R inv = (R)bs_[0];
     SEG_LOOP(i) {
         cx<R> v = VT<V>::ld(in, i);
         VT<V>::st(out, i, {v.re * inv, v.im * inv});
     }
 }
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_normalize(SEG seg, const V *in, V *out, int nslot) {
+    d_normalize<V, SEG>(seg, in, out, nslot);
+}
 
 // v <- v - x ip0 - y ip1 (ip from red[kIp0], red[kIp1]); red[kVn] = |v|^2
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_sub2_norm(SEG seg, const V *x, const V *y, V *v) {
+__device__ __forceinline__ void d_sub2_norm(SEG seg, const V *x, const V *y, V *v) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -269,19 +287,26 @@ k_sub2_norm(SEG seg, const V *x, const V *y, V *v) {
         VT<V>::st(v, i, w);
         nn.add(w, w, VT<V>::kComplex);
     }
-    double2 r[1] = {nn.get()};
+    cdf r[1] = {nn.get_cdf()};
     seg.template reduce<1>(r, kVn);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_sub2_norm(SEG seg, const V *x, const V *y, V *v) {
+    d_sub2_norm<V, SEG>(seg, x, y, v);
 }
 
 // v <- v / (|v| or 1); red[kIp0] = <x, v>, red[kIp1] = <y, v>
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_scale_dots2(SEG seg, const V *x, const V *y, V *v, int do_scale) {
+__device__ __forceinline__ void d_scale_dots2(SEG seg, const V *x, const V *y, V *v, int do_scale) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const double n = sqrt(st->red[kVn].x);
-    const R inv = (R)((!do_scale || n == 0.) ? 1. : 1. / n);
+    BLOCK_SCALARS(1, {
+        const double n = sqrt(st->red[kVn].x);
+        out[0] = (!do_scale || n == 0.) ? 1. : 1. / n;
+    })
+    const R inv = (R)bs_[0];
     CDot<R> d0, d1;
     SEG_LOOP(i) {
         cx<R> w = VT<V>::ld(v, i);
@@ -290,28 +315,37 @@ k_scale_dots2(SEG seg, const V *x, const V *y, V *v, int do_scale) {
         d0.add(VT<V>::ld(x, i), w, VT<V>::kComplex);
         d1.add(VT<V>::ld(y, i), w, VT<V>::kComplex);
     }
-    double2 r[2] = {d0.get(), d1.get()};
+    cdf r[2] = {d0.get_cdf(), d1.get_cdf()};
     seg.template reduce<2>(r, kIp0);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_scale_dots2(SEG seg, const V *x, const V *y, V *v, int do_scale) {
+    d_scale_dots2<V, SEG>(seg, x, y, v, do_scale);
 }
 
 // p = v if |v| >= 0.99 else 0 (ground_locg.py:421)
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_mask(SEG seg, const V *v, V *p) {
+__device__ __forceinline__ void d_mask(SEG seg, const V *v, V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const R m = (R)(sqrt(st->red[kVn].x) >= 0.99 ? 1. : 0.);
+    BLOCK_SCALARS(1, { out[0] = sqrt(st->red[kVn].x) >= 0.99 ? 1. : 0.; })
+    const R m = (R)bs_[0];
     SEG_LOOP(i) {
         cx<R> w = VT<V>::ld(v, i);
         VT<V>::st(p, i, {w.re * m, w.im * m});
     }
 }
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_mask(SEG seg, const V *v, V *p) {
+    d_mask<V, SEG>(seg, v, p);
+}
 
 // Gram entries of (x, y, p): <y,Ax> <p,Ax> <p,Ay> <x,Ax> <y,Ay> <p,Ap>
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_gram3(SEG seg, const V *x, const V *y, const V *p, const V *ax, const V *ay,
+__device__ __forceinline__ void d_gram3(SEG seg, const V *x, const V *y, const V *p, const V *ax, const V *ay,
         const V *ap) {
     State *st = seg.state();
     GATE(st);
@@ -328,16 +362,21 @@ k_gram3(SEG seg, const V *x, const V *y, const V *p, const V *ax, const V *ay,
         g[4].add(yi, ayi, c);
         g[5].add(pi, api, c);
     }
-    double2 r[6];
+    cdf r[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) r[k] = g[k].get();
+    for (int k = 0; k < 6; ++k) r[k] = g[k].get_cdf();
     seg.template reduce<6>(r, kG10);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_gram3(SEG seg, const V *x, const V *y, const V *p, const V *ax, const V *ay,
+        const V *ap) {
+    d_gram3<V, SEG>(seg, x, y, p, ax, ay, ap);
 }
 
 // Gram entries of (x, p) for the first Rayleigh-Ritz step: <p,Ax> <x,Ax> <p,Ap>
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_gram2(SEG seg, const V *x, const V *p, const V *ax, const V *ap) {
+__device__ __forceinline__ void d_gram2(SEG seg, const V *x, const V *p, const V *ax, const V *ap) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -350,14 +389,18 @@ k_gram2(SEG seg, const V *x, const V *p, const V *ax, const V *ap) {
         g[1].add(xi, axi, c);
         g[2].add(pi, api, c);
     }
-    double2 r[3] = {g[0].get(), g[1].get(), g[2].get()};
+    cdf r[3] = {g[0].get_cdf(), g[1].get_cdf(), g[2].get_cdf()};
     seg.template reduce<3>(r, kG10);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_gram2(SEG seg, const V *x, const V *p, const V *ax, const V *ap) {
+    d_gram2<V, SEG>(seg, x, p, ax, ap);
 }
 
 // s = k1 y + k2 p: red[kSn] = |s|^2
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_upd_s(SEG seg, const V *y, const V *p) {
+__device__ __forceinline__ void d_upd_s(SEG seg, const V *y, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -367,21 +410,31 @@ k_upd_s(SEG seg, const V *y, const V *p) {
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
         nn.add(s, s, VT<V>::kComplex);
     }
-    double2 r[1] = {nn.get()};
+    cdf r[1] = {nn.get_cdf()};
     seg.template reduce<1>(r, kSn);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_upd_s(SEG seg, const V *y, const V *p) {
+    d_upd_s<V, SEG>(seg, y, p);
 }
 
 // t = s (k0/|s|) - x |s|, u = k0 x + s: red[kTn] = |t|^2, red[kUn] = |u|^2
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_upd_tu(SEG seg, const V *x, const V *y, const V *p) {
+__device__ __forceinline__ void d_upd_tu(SEG seg, const V *x, const V *y, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const double ns = sqrt(st->red[kSn].x);
+    BLOCK_SCALARS(3, {
+        const double ns = sqrt(st->red[kSn].x);
+        out[0] = ns;
+        out[1] = st->kappa[0].x / ns;
+        out[2] = st->kappa[0].y / ns;
+    })
+    const double ns = bs_[0];
     const bool keep_y = st->guard && ns == 0.;  // s = 0: y' = y instead of 0 * inf
     const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
-    const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
+    const cx<R> k0s = c_of<R>(make_double2(bs_[1], bs_[2]));
     const cx<R> mns = {(R)(-ns), (R)0};
     CDot<R> tn, un;
     SEG_LOOP(i) {
@@ -392,24 +445,35 @@ k_upd_tu(SEG seg, const V *x, const V *y, const V *p) {
         tn.add(t, t, VT<V>::kComplex);
         un.add(u, u, VT<V>::kComplex);
     }
-    double2 r[2] = {tn.get(), un.get()};
+    cdf r[2] = {tn.get_cdf(), un.get_cdf()};
     seg.template reduce<2>(r, kTn);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_upd_tu(SEG seg, const V *x, const V *y, const V *p) {
+    d_upd_tu<V, SEG>(seg, x, y, p);
 }
 
 // x <- u / |u|, y <- t / |t|; FAST also carries A x, A y by the same combinations.
 template <typename V, bool CARRY, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
+__device__ __forceinline__ void d_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const double ns = sqrt(st->red[kSn].x);
+    BLOCK_SCALARS(5, {
+        const double ns = sqrt(st->red[kSn].x);
+        out[0] = ns;
+        out[1] = st->kappa[0].x / ns;
+        out[2] = st->kappa[0].y / ns;
+        out[3] = 1. / sqrt(st->red[kTn].x);
+        out[4] = 1. / sqrt(st->red[kUn].x);
+    })
+    const double ns = bs_[0];
     const bool keep_y = st->guard && ns == 0.;  // s = 0: y' = y instead of 0 * inf
-    const double it = 1. / sqrt(st->red[kTn].x), iu = 1. / sqrt(st->red[kUn].x);
     const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
-    const cx<R> k0s = c_of<R>(make_double2(st->kappa[0].x / ns, st->kappa[0].y / ns));
+    const cx<R> k0s = c_of<R>(make_double2(bs_[1], bs_[2]));
     const cx<R> mns = {(R)(-ns), (R)0};
-    const R rit = (R)it, riu = (R)iu;
+    const R rit = (R)bs_[3], riu = (R)bs_[4];
     SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i);
         const cx<R> yi = VT<V>::ld(y, i);
@@ -429,11 +493,15 @@ k_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
         }
     }
 }
+template <typename V, bool CARRY, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
+    d_upd_xy<V, CARRY, SEG>(seg, x, y, p, ax, ay, ap);
+}
 
 // iteration 1 update (ground_locg.py:278-281): t = p k0 - x k1, u = x k0 + p k1 -> norms
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_upd2_norms(SEG seg, const V *x, const V *p) {
+__device__ __forceinline__ void d_upd2_norms(SEG seg, const V *x, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -447,13 +515,17 @@ k_upd2_norms(SEG seg, const V *x, const V *p) {
         tn.add(t, t, VT<V>::kComplex);
         un.add(u, u, VT<V>::kComplex);
     }
-    double2 r[2] = {tn.get(), un.get()};
+    cdf r[2] = {tn.get_cdf(), un.get_cdf()};
     seg.template reduce<2>(r, kTn);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_upd2_norms(SEG seg, const V *x, const V *p) {
+    d_upd2_norms<V, SEG>(seg, x, p);
 }
 
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_upd2_xy(SEG seg, V *x, V *y, const V *p) {
+__device__ __forceinline__ void d_upd2_xy(SEG seg, V *x, V *y, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -468,12 +540,16 @@ k_upd2_xy(SEG seg, V *x, V *y, const V *p) {
         VT<V>::st(y, i, {t.re * rit, t.im * rit});
     }
 }
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_upd2_xy(SEG seg, V *x, V *y, const V *p) {
+    d_upd2_xy<V, SEG>(seg, x, y, p);
+}
 
 // r = Ax - theta x; red[kAxn] = |Ax|^2, red[kRn] = |r|^2.  theta from st->theta, or from
 // Re red[kMisc] (iteration 0: rho = Re <x, Ax>) when use_rho.
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_resid(SEG seg, const V *ax, const V *x, V *r, int use_rho) {
+__device__ __forceinline__ void d_resid(SEG seg, const V *ax, const V *x, V *r, int use_rho) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -487,14 +563,18 @@ k_resid(SEG seg, const V *ax, const V *x, V *r, int use_rho) {
         an.add(a, a, VT<V>::kComplex);
         rn.add(w, w, VT<V>::kComplex);
     }
-    double2 out[2] = {an.get(), rn.get()};
+    cdf out[2] = {an.get_cdf(), rn.get_cdf()};
     seg.template reduce<2>(out, kAxn);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_resid(SEG seg, const V *ax, const V *x, V *r, int use_rho) {
+    d_resid<V, SEG>(seg, ax, x, r, use_rho);
 }
 
 // w = r / (d - theta), |d - theta| floored at 1e-8 (1 + |theta|): the Jacobi preconditioner.
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads)
-k_jacobi(SEG seg, const double *diag, const V *r, V *w) {
+__device__ __forceinline__ void d_jacobi(SEG seg, const double *diag, const V *r, V *w) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
@@ -507,6 +587,11 @@ k_jacobi(SEG seg, const double *diag, const V *r, V *w) {
         const cx<R> v = VT<V>::ld(r, i);
         VT<V>::st(w, i, {v.re * f, v.im * f});
     }
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads)
+k_jacobi(SEG seg, const double *diag, const V *r, V *w) {
+    d_jacobi<V, SEG>(seg, diag, r, w);
 }
 
 template <typename VS, typename VD>
@@ -523,9 +608,10 @@ __global__ void __launch_bounds__(kThreads) k_convert(int64_t D, const VS *a, VD
 // ------------------------------------------------------------------------------------------
 // scalar kernels: one thread per problem
 // ------------------------------------------------------------------------------------------
+// scalar steps: problem p_ = first, first + step, ... (one thread per problem in the kernels; the
+// persistent kernel runs them on thread 0 of every block, on the block's own copy of the state)
 #define FOR_ACTIVE_PROBLEMS(states, P, st)                                          \
-    for (int p_ = blockIdx.x * blockDim.x + threadIdx.x; p_ < (P);              \
-         p_ += gridDim.x * blockDim.x)                                             \
+    for (int p_ = first; p_ < (P); p_ += step)                                     \
         for (State *st = (states) + p_; st != nullptr && st->active; st = nullptr)
 
 // Lowest eigenpair of a Hermitian 3x3 given by its strict lower triangle (m10, m20, m21) and its
@@ -600,7 +686,7 @@ __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2
     for (int k = 0; k < 3; ++k) v[k] = make_double2(c[k].x / nrm, c[k].y / nrm);
 }
 
-__global__ void k_rr3(State *states, int P) {
+__device__ __forceinline__ void d_rr3(State *states, int P, int first, int step) {
     FOR_ACTIVE_PROBLEMS(states, P, st) {
         double lam;
         double2 v[3];
@@ -611,9 +697,10 @@ __global__ void k_rr3(State *states, int P) {
         break;
     }
 }
+__global__ void k_rr3(State *states, int P) { d_rr3(states, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x); }
 
 // eigenpair_2x2 (ground_locg.py:424-435) of [[g00, conj(g10)], [g10, g11]]
-__global__ void k_rr2(State *states, int P) {
+__device__ __forceinline__ void d_rr2(State *states, int P, int first, int step) {
     FOR_ACTIVE_PROBLEMS(states, P, st) {
     // k_gram2 wrote <p,Ax>, <x,Ax>, <p,Ap> to three consecutive slots from kG10
     const double2 m10 = st->red[kG10];
@@ -633,12 +720,13 @@ __global__ void k_rr2(State *states, int P) {
     break;
     }
 }
+__global__ void k_rr2(State *states, int P) { d_rr2(states, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x); }
 
 // iteration 0: rho = Re <x, Ax> into red[kMisc] (already there from k_dots); nothing else.
 
 // Convergence test of ground_locg.py:329-334 and phase bookkeeping; a problem that stops
 // decrements the count of active problems.
-__global__ void k_check(State *states, int P, int *nactive) {
+__device__ __forceinline__ void d_check(State *states, int P, int *nactive, int first, int step) {
     FOR_ACTIVE_PROBLEMS(states, P, st) {
     const double rn = sqrt(st->red[kRn].x);
     const double an = sqrt(st->red[kAxn].x);
@@ -679,14 +767,17 @@ __global__ void k_check(State *states, int P, int *nactive) {
     st->converged = conv ? 1 : 0;
     if (conv || st->iter >= st->maxiter) {
         st->active = 0;
-        atomicSub(nactive, 1);
+        if (nactive) atomicSub(nactive, 1);
     }
     break;
     }
 }
+__global__ void k_check(State *states, int P, int *nactive) {
+    d_check(states, P, nactive, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
 
 // FAST: a refresh starts -- reset the counter (runs only when want_refresh is set)
-__global__ void k_refresh_mark(State *states, int P) {
+__device__ __forceinline__ void d_refresh_mark(State *states, int P, int first, int step) {
     FOR_ACTIVE_PROBLEMS(states, P, st) {
         if (st->want_refresh) {
             st->since_refresh = 0;
@@ -694,6 +785,9 @@ __global__ void k_refresh_mark(State *states, int P) {
         }
         break;
     }
+}
+__global__ void k_refresh_mark(State *states, int P) {
+    d_refresh_mark(states, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -725,7 +819,7 @@ Layout layout(int64_t D, const rq_lobpcg_params_t &p) {
         return o;
     };
     L.state = take(sizeof(State));
-    L.err = take(16);
+    L.err = take(64);  // [0] matvec error flag, [8] active count, [16] grid barrier
     L.red = take(reduce_scratch_bytes());
     L.hi_bytes = (size_t)D * vtype_size(p.vtype);
     L.lo_bytes = (size_t)D * vtype_size(lo_type(p.vtype));
@@ -793,6 +887,10 @@ struct Phase {
     Vecs<V> v;
     bool jacobi;
     const double *diag;
+    // set when the loop may run as one persistent cooperative kernel (one problem, cached
+    // connectivity or CSR operator of this phase's value type)
+    const rq_operator_t *pop = nullptr;
+    GridBar *bar = nullptr;
 
     int pgrid() const { return (P + 127) / 128; }
 
@@ -930,6 +1028,241 @@ int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s) {
     return rc;
 }
 
+// ------------------------------------------------------------------------------------------
+// Persistent LOBPCG: one cooperative launch runs a phase's iterations to convergence.  The passes
+// are the same device bodies as the kernels above, separated by a grid barrier instead of a
+// kernel boundary (a launch and its drain cost more than the work of a pass at D <= 2^20).
+// ------------------------------------------------------------------------------------------
+constexpr long long kBarrierCycles = 4000000000LL;  // ~2 s at 2 GHz: a barrier that waits longer aborts
+
+// Grid barrier on a counter that only grows: each block adds 1 without waiting for the old value
+// (the adds pipeline in L2 instead of queueing for their results) and waits until the counter
+// reaches (barriers passed) x (blocks); `passed` is the block's own count, kept in shared
+// memory.  Every wait is bounded; a block that gives up raises `abort`, which releases every
+// other waiter at once.  Returns false after an abort.
+__device__ bool grid_sync(GridBar *b, unsigned int *passed) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned int target = (*passed + 1u) * gridDim.x;
+        *passed += 1u;
+        volatile unsigned int *count = &b->count;
+        volatile int *abort = &b->abort;
+        __threadfence();
+        atomicAdd(&b->count, 1u);
+        const long long t0 = clock64();
+        while ((int)(*count - target) < 0) {
+            if (*abort) {
+                ok = 0;
+                break;
+            }
+            if (clock64() - t0 > kBarrierCycles) {
+                atomicExch(&b->abort, 1);
+                ok = 0;
+                break;
+            }
+        }
+        __threadfence();
+        if (*abort) ok = 0;
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// One problem inside the persistent kernel: every block holds its own copy of the solver state
+// in shared memory.  A reduction writes the block's partial sums, crosses one grid barrier and
+// then every block adds all partials itself in the same order, so the copies stay identical
+// without a second barrier; scalar steps run on each block's thread 0.  Element i is always
+// handled by the same thread, so passes that only touch a thread's own elements need no barrier.
+struct SegPersist {
+    State *st;      // this block's shared-memory copy
+    int64_t D;
+    float4 *part;   // [2][gridDim.x * kMaxReduce] partial sums, alternate reductions alternate
+                    // halves (a block may write the next sums while another still reads these)
+    GridBar *bar;
+    int *flip;      // shared: which half the next reduction uses
+    unsigned int *passed;  // shared: barriers this block has passed
+    __device__ __forceinline__ State *state() const { return st; }
+    __device__ __forceinline__ int64_t begin() const {
+        return blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    }
+    __device__ __forceinline__ int64_t end() const { return D; }
+    __device__ __forceinline__ int64_t stride() const { return (int64_t)gridDim.x * blockDim.x; }
+    template <int NV>
+    __device__ void reduce(cdf (&v)[NV], int slot) const {
+        __shared__ cdf red[kThreads / 32][NV];
+        cdf w[NV];
+        float4 *pb = part + (size_t)(*flip) * gridDim.x * kMaxReduce;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) w[k] = v[k];
+        block_sum<NV>(w, red);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) pb[(size_t)blockIdx.x * kMaxReduce + k] = cdf_pack(w[k]);
+        }
+        if (!grid_sync(bar, passed)) {
+            if (threadIdx.x == 0) st->active = 0;  // aborted: every block stops
+            __syncthreads();
+            return;
+        }
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            cdf acc = cdf_zero();
+            for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+                acc = cdf_add(acc, cdf_unpack(__ldcg(pb + (size_t)b * kMaxReduce + k)));
+            w[k] = acc;
+        }
+        __syncthreads();  // red[] reuse
+        block_sum<NV>(w, red);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) st->red[slot + k] = cdf_val(w[k]);
+            *flip ^= 1;
+        }
+        __syncthreads();
+    }
+};
+
+template <typename V>
+struct PersistArgs {
+    State *st;      // global state (read at start, written back by block 0 at the end)
+    int64_t D;
+    float4 *part;
+    rq_operator_t op;
+    Vecs<V> v;
+    int variant;
+    int jacobi;
+    const double *diag;
+    GridBar *bar;
+};
+
+// MVK 0: cached connectivity, 1: CSR with values of type V
+template <typename V, int MVK>
+__device__ __forceinline__ void persist_mv(const PersistArgs<V> &a, State *st, const V *in, V *out,
+                                           const int *gate2) {
+    if (MVK == 0)
+        d_matvec_conn<V>(a.op, in, out, &st->active, gate2);
+    else
+        d_matvec_csr<V, V>(a.op, in, out, &st->active, gate2);
+}
+
+template <typename V, int MVK>
+__global__ void __launch_bounds__(kThreads) k_persist(const PersistArgs<V> a) {
+    __shared__ State sst;
+    __shared__ int flip;
+    __shared__ unsigned int passed;
+    if (threadIdx.x == 0) {
+        flip = 0;
+        passed = 0u;
+    }
+    {
+        const int n = (int)(sizeof(State) / sizeof(int));
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            reinterpret_cast<int *>(&sst)[k] = reinterpret_cast<const int *>(a.st)[k];
+    }
+    __syncthreads();
+    State *st = &sst;
+    const SegPersist seg{st, a.D, a.part, a.bar, &flip, &passed};
+    const Vecs<V> v = a.v;
+    constexpr int kOnce = 1 << 30;  // step of the scalar loops: thread 0 only
+    auto sync = [&]() -> bool {
+        if (grid_sync(a.bar, &passed)) return true;
+        if (threadIdx.x == 0) st->active = 0;
+        __syncthreads();
+        return false;
+    };
+    auto scalar_done = [&]() { __syncthreads(); };
+    while (st->active) {
+        V *src = v.r;
+        if (a.jacobi) {
+            d_jacobi<V, SegPersist>(seg, a.diag, v.r, v.w);
+            src = v.w;
+        }
+        // project_out((x, y), src) -> p
+        Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
+        d_dots<V, 2, SegPersist>(seg, pr, kIp0);
+        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+        d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
+        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+        d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
+        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+        d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 0);
+        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+        d_mask<V, SegPersist>(seg, src, v.p);
+        if (!sync()) break;  // the products gather p (and x, y) from every block's rows
+        if (a.variant == RQ_LOBPCG_REFERENCE) {
+            persist_mv<V, MVK>(a, st, v.x, v.ax, nullptr);
+            persist_mv<V, MVK>(a, st, v.y, v.ay, nullptr);
+        }
+        persist_mv<V, MVK>(a, st, v.p, v.ap, nullptr);
+        d_gram3<V, SegPersist>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+        if (threadIdx.x == 0) d_rr3(st, 1, 0, kOnce);
+        scalar_done();
+        d_upd_s<V, SegPersist>(seg, v.y, v.p);
+        d_upd_tu<V, SegPersist>(seg, v.x, v.y, v.p);
+        if (a.variant == RQ_LOBPCG_REFERENCE) {
+            d_upd_xy<V, false, SegPersist>(seg, v.x, v.y, v.p, nullptr, nullptr, nullptr);
+            if (!sync()) break;
+            persist_mv<V, MVK>(a, st, v.x, v.ax, nullptr);
+        } else {
+            d_upd_xy<V, true, SegPersist>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+            if (st->want_refresh) {
+                if (!sync()) break;
+                persist_mv<V, MVK>(a, st, v.x, v.ax, &st->want_refresh);
+                persist_mv<V, MVK>(a, st, v.y, v.ay, &st->want_refresh);
+                if (threadIdx.x == 0) d_refresh_mark(st, 1, 0, kOnce);
+                scalar_done();
+            }
+        }
+        d_resid<V, SegPersist>(seg, v.ax, v.x, v.r, 0);
+        if (threadIdx.x == 0) d_check(st, 1, nullptr, 0, kOnce);
+        scalar_done();
+    }
+    // the copies are identical; block 0 publishes its own
+    if (blockIdx.x == 0) {
+        const int n = (int)(sizeof(State) / sizeof(int));
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            reinterpret_cast<int *>(a.st)[k] = reinterpret_cast<const int *>(&sst)[k];
+    }
+}
+
+template <typename PH>
+int run_persist(PH &ph, int variant, cudaStream_t s) {
+    using V = typename std::remove_pointer<decltype(ph.v.x)>::type;
+    const rq_operator_t &op = *ph.pop;
+    const void *kern = op.mode == RQ_MODE_CONN ? (const void *)k_persist<V, 0> : (const void *)k_persist<V, 1>;
+    int per = 0;
+    RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, 0));
+    if (per < 1) return run_loop(ph, variant, true, kChunk, s);
+    int grid = ph.grid;
+    if (grid > per * sm_count()) grid = per * sm_count();
+    if (grid > kMaxReduceBlocks / 2) grid = kMaxReduceBlocks / 2;  // two halves of partial sums
+    // partial sums in the phase's reduction scratch (its counter slot stays unused)
+    float4 *part = reinterpret_cast<float4 *>(static_cast<char *>(ph.seg.red) + 16);
+    PersistArgs<V> a{ph.states, ph.seg.D, part, op, ph.v, variant, ph.jacobi ? 1 : 0, ph.diag,
+                     ph.bar};
+    RQ_CUDA(cudaMemsetAsync(ph.bar, 0, sizeof(GridBar), s));
+    void *args[] = {&a};
+    RQ_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, s));
+    GridBar h{};
+    RQ_CUDA(cudaMemcpyAsync(&h, ph.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
+    RQ_CUDA(cudaStreamSynchronize(s));
+    if (h.abort) return fail(RQ_E_CUDA, "persistent LOBPCG: a grid barrier timed out");
+    return RQ_OK;
+}
+
+// The iterations of one phase: a persistent kernel when the phase allows it, else CUDA-graph
+// chunks (or eager launches).
+template <typename PH>
+int run_iterations(PH &ph, int variant, bool graph, int chunk, cudaStream_t s) {
+    if constexpr (std::is_same<typename std::decay<decltype(ph.seg)>::type, SegOne>::value) {
+        if (graph && ph.pop && ph.bar) return run_persist(ph, variant, s);
+    }
+    return run_loop(ph, variant, graph, chunk, s);
+}
+
 // Per-problem state initialisation (tol_dim per problem), and the count of active problems.
 int init_states(State *dev, int *nactive, int P, const rq_lobpcg_params_t &p, double tol,
                 const std::vector<double> &tol_dim, bool lo, cudaStream_t s) {
@@ -985,7 +1318,7 @@ int run_phases(PLO &lo, PHI &hi, bool mixed, const rq_lobpcg_params_t &p, double
         RQ_TRY(init_states(lo.states, lo.nactive, P, p, eps_of(lo.vtype), tol_dim, true, s));
         k_convert<VHI, VLO><<<gconv, kThreads, 0, s>>>(D, static_cast<const VHI *>(x0), lo.v.x);
         RQ_TRY(lo.start(p.variant, s));
-        if (p.maxiter > 0) RQ_TRY(run_loop(lo, p.variant, graph, chunk, s));
+        if (p.maxiter > 0) RQ_TRY(run_iterations(lo, p.variant, graph, chunk, s));
         std::vector<State> h(P);
         RQ_CUDA(cudaMemcpyAsync(h.data(), lo.states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
         RQ_CUDA(cudaStreamSynchronize(s));
@@ -1006,7 +1339,7 @@ int run_phases(PLO &lo, PHI &hi, bool mixed, const rq_lobpcg_params_t &p, double
         RQ_CUDA(cudaMemcpyAsync(hi.v.x, x0, hi_bytes, cudaMemcpyDeviceToDevice, s));
         RQ_TRY(hi.start(p.variant, s));
     }
-    if (p.maxiter > 0) RQ_TRY(run_loop(hi, p.variant, graph, chunk, s));
+    if (p.maxiter > 0) RQ_TRY(run_iterations(hi, p.variant, graph, chunk, s));
     return RQ_OK;
 }
 
@@ -1018,7 +1351,7 @@ int solve(const rq_operator_t &op, MV mv, bool callback, const rq_lobpcg_params_
     State *st = reinterpret_cast<State *>(ws + L.state);
     int *nactive = reinterpret_cast<int *>(ws + L.err + 8);
     void *red = ws + L.red;
-    RQ_CUDA(cudaMemsetAsync(ws + L.err, 0, 16, s));
+    RQ_CUDA(cudaMemsetAsync(ws + L.err, 0, 64, s));
     RQ_CUDA(cudaMemsetAsync(red, 0, 16, s));
     const std::vector<double> tol_dim(1, p.tol_dim > 0 ? p.tol_dim : (double)D);
     const bool jac = p.jacobi != 0 && op.diag0 != nullptr;
@@ -1034,6 +1367,18 @@ int solve(const rq_operator_t &op, MV mv, bool callback, const rq_lobpcg_params_
                               jac, op.diag0};
     std::vector<int> nlo;
     const bool graph = p.use_graph != 0 && !callback;
+    if (graph && p.use_graph != 2 && (op.mode == RQ_MODE_CONN || op.mode == RQ_MODE_CSR)) {
+        // one persistent kernel per phase; CSR values must be of the phase's own type
+        GridBar *bar = reinterpret_cast<GridBar *>(ws + L.err + 16);
+        if (op.mode == RQ_MODE_CONN || op.val_vtype == hi_type) {
+            hi.pop = &op;
+            hi.bar = bar;
+        }
+        if (op.mode == RQ_MODE_CONN || op.val_vtype == lo.vtype) {
+            lo.pop = &op;
+            lo.bar = bar;
+        }
+    }
     RQ_TRY(run_phases(lo, hi, mixed, p, tol, tol_dim, D, x0, L.hi_bytes, callback ? 1 : kChunk,
                       graph, s, nlo));
     State h{};

@@ -13,6 +13,7 @@
 #include <cmath>
 
 #include "rq_common.cuh"
+#include "rq_rows.cuh"
 #include "rq_host.h"
 
 namespace rq {
@@ -127,8 +128,9 @@ __device__ __forceinline__ void for_hits(const rq_subspace_t &S, const uint32_t 
             if (!sector_ok(fb, S.fmask_a, S.fmask_b, t)) continue;
             if (LK == RQ_LOOKUP_HASH) {
                 if (KB == 32 && (t >> 32) != 0) continue;
-                m = lookup_hash_at<KB>(
-                    S, t, bucket_from_hash(lin_hash(T, t, KeyWidth<KB>::kNbytes), S.hbits), err);
+                const uint32_t h = lin_hash(T, t, KeyWidth<KB>::kNbytes);
+                if (S.pbits > 0 && S.pmap && !present(S.pmap, h, S.pbits)) continue;
+                m = lookup_hash_at<KB>(S, t, bucket_from_hash(h, S.hbits), err);
             } else {
                 m = lookup_bsearch(S, samp, ns, t);
             }
@@ -157,8 +159,6 @@ __device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, ui
 // together; the loop only marks "hot" groups (a key match, a full bucket, or a target equal to
 // the empty key) in a 64-bit mask, resolved once per 64 groups so that the rare divergent work
 // is not interleaved with the probes.
-template <typename R>
-__device__ __forceinline__ cx<R> group_diag(const rq_terms_t &T, int g, uint64_t s);
 
 // Group keys live in shared memory for the whole launch: (x_j, h(x_j)) packed as uint2 for 32-bit
 // keys (8 B per group) or as uint64 + uint32 arrays for 64-bit keys (12 B per group).  Large J
@@ -210,6 +210,8 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
     const bool d0 = (op.diag0 != nullptr) && (skip >= 0);
     const K fa = (K)S.fmask_a, fbm = (K)S.fmask_b, empty = (K)S.empty_key;
     const int shift = 32 - S.hbits;
+    const uint32_t *pmap = S.pbits > 0 ? S.pmap : nullptr;
+    const int pshift = 32 - S.pbits;
     const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
     // Every lane runs the same row batches and super-chunks (lanes past D with nothing to do),
     // so that the warp can be re-converged after each super-chunk's hot-group resolution; without
@@ -252,11 +254,21 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
                     }
                     q[u] = active && (g + u != skip);
                     if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
-                    b[u] = (hs ^ hxg) >> shift;
+                    b[u] = hs ^ hxg;
+                }
+                if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
+                    uint32_t pw[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const uint32_t idx = b[u] >> pshift;
+                        pw[u] = q[u] ? __ldg(pmap + (idx >> 5)) : 0u;
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) q[u] = q[u] && ((pw[u] >> ((b[u] >> pshift) & 31)) & 1u);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    w[u] = KeyWidth<KB>::load(keys + (size_t)b[u] * kBucketBytes, q[u],
+                    w[u] = KeyWidth<KB>::load(keys + (size_t)(b[u] >> shift) * kBucketBytes, q[u],
                                               S.empty_key);
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
@@ -388,18 +400,7 @@ k_conn_count(const rq_operator_t op, int64_t *__restrict__ rowcnt, int *err) {
 }
 
 // Diagonal of group g for state s from the global term arrays (CONN mode and CSR values).
-template <typename R>
-__device__ __forceinline__ cx<R> group_diag(const rq_terms_t &T, int g, uint64_t s) {
-    CAcc<R> d;
-    const int k1 = __ldg(T.toff + g + 1);
-    for (int k = __ldg(T.toff + g); k < k1; ++k) {
-        const R re = (R)__ldg(T.coef + 2 * k), im = (R)__ldg(T.coef + 2 * k + 1);
-        if (re == (R)0 && im == (R)0) break;
-        if (__popcll(s & __ldg(T.zmask + k)) & 1) d.add({-re, -im});
-        else d.add({re, im});
-    }
-    return d.get();
-}
+
 
 template <typename V, int LK, int KB>
 __global__ void __launch_bounds__(kThreads)
@@ -513,25 +514,7 @@ template <typename V>
 __global__ void __launch_bounds__(kThreads)
 k_matvec_conn(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, const int *gate,
               const int *gate2) {
-    using R = typename VT<V>::R;
-    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
-    const rq_terms_t &T = op.terms;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.sub.D;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t s = __ldg(op.sub.states + i);
-        CAcc<R> acc;
-        const cx<R> xi = VT<V>::ld(x, i);
-        if (op.diag0) {
-            const R dv = (R)op.diag0[i];
-            acc.add({dv * xi.re, dv * xi.im});
-        } else if (T.diag_group >= 0) {
-            acc.add(cmul(group_diag<R>(T, T.diag_group, s), xi));
-        }
-        const int64_t e1 = op.rowptr[i + 1];
-        for (int64_t e = op.rowptr[i]; e < e1; ++e)
-            acc.add(cmul(group_diag<R>(T, __ldg(op.grp + e), s), VT<V>::ld(x, __ldg(op.col + e))));
-        VT<V>::st(y, i, acc.get());
-    }
+    d_matvec_conn<V>(op, x, y, gate, gate2);
 }
 
 // VV: storage type of the element values (converted to the vector's precision on load)
@@ -539,24 +522,7 @@ template <typename V, typename VV>
 __global__ void __launch_bounds__(kThreads)
 k_matvec_csr(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, const int *gate,
              const int *gate2) {
-    using R = typename VT<V>::R;
-    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
-    const VV *val = reinterpret_cast<const VV *>(op.val);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.sub.D;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        CAcc<R> acc;
-        if (op.diag0) {
-            const R dv = (R)op.diag0[i];
-            const cx<R> xi = VT<V>::ld(x, i);
-            acc.add({dv * xi.re, dv * xi.im});
-        }
-        const int64_t e1 = op.rowptr[i + 1];
-        for (int64_t e = op.rowptr[i]; e < e1; ++e) {
-            const auto v = VT<VV>::ld(val, e);
-            acc.add(cmul(cx<R>{(R)v.re, (R)v.im}, VT<V>::ld(x, __ldg(op.col + e))));
-        }
-        VT<V>::st(y, i, acc.get());
-    }
+    d_matvec_csr<V, VV>(op, x, y, gate, gate2);
 }
 
 template <typename V>

@@ -41,6 +41,19 @@ __global__ void k_fill_u64(uint64_t *p, int64_t n, uint64_t v) {
 // Insert every state into its bucket chain: claim the first empty slot with a CAS.  Keys are
 // distinct, so a failed CAS always means "occupied by another key".  Slots of a bucket are
 // claimed in order, which keeps the occupied slots a prefix of the bucket.
+// presence bitmap: bit (hash(key) >> (32 - pbits)) for every key
+template <int KB>
+__global__ void k_pmap_build(const uint64_t *__restrict__ keys, int64_t D, uint32_t *pmap, int pbits) {
+    __shared__ uint32_t T[kHashTableWords];
+    init_hash_tables(T, KeyWidth<KB>::kNbytes);
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t idx = lin_hash(T, keys[i], KeyWidth<KB>::kNbytes) >> (32 - pbits);
+        atomicOr(pmap + (idx >> 5), 1u << (idx & 31));
+    }
+}
+
 template <int KB>
 __global__ void __launch_bounds__(kThreads)
 k_hash_insert(const uint64_t *__restrict__ states, int64_t D, void *keys, int32_t *vals, int hbits,
@@ -188,7 +201,7 @@ int grid_for(int64_t n, int per_sm = 8) {
 // rq_subspace_build and rq_batch_build.  `flag` and `gap` are device scratch words.
 int build_key_table(const uint64_t *keys, int64_t D, int key_bits, bool hash, void *hkeys,
                     int32_t *hvals, int hbits, uint64_t *empty_out, int *flag,
-                    unsigned long long *gap, cudaStream_t st) {
+                    unsigned long long *gap, cudaStream_t st, uint32_t *pmap, int pbits) {
     RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     RQ_CUDA(cudaMemsetAsync(gap, 0xff, sizeof(unsigned long long), st));
     k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(keys, D, flag);
@@ -233,6 +246,14 @@ int build_key_table(const uint64_t *keys, int64_t D, int key_bits, bool hash, vo
                                                                 flag);
         }
         RQ_CUDA(cudaGetLastError());
+        if (pmap && pbits > 0) {
+            RQ_CUDA(cudaMemsetAsync(pmap, 0, ((size_t)1 << pbits) / 8, st));
+            if (key_bits == 64)
+                k_pmap_build<64><<<grid_for(D), kThreads, 0, st>>>(keys, D, pmap, pbits);
+            else
+                k_pmap_build<32><<<grid_for(D), kThreads, 0, st>>>(keys, D, pmap, pbits);
+            RQ_CUDA(cudaGetLastError());
+        }
         int h_err = 0;
         RQ_CUDA(cudaMemcpyAsync(&h_err, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         RQ_CUDA(cudaStreamSynchronize(st));
@@ -252,6 +273,16 @@ RQ_API int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits) {
     while ((int64_t(1) << b) * kBucketSlots < 8 * D) ++b;  // load factor <= 1/8
     if (b > 31) return fail(RQ_E_RANGE, "rq_subspace_sizes: D too large");
     *hbits = b;
+    return RQ_OK;
+}
+
+RQ_API int rq_presence_bits(int64_t D, int32_t key_bits, int32_t *pbits) {
+    if (!pbits) return fail(RQ_E_ARG, "rq_presence_bits: null argument");
+    int32_t hb = 0;
+    RQ_TRY(rq_subspace_sizes(D, key_bits, &hb));
+    const double table = (double)(key_bits / 8) * kBucketSlots * (double)(int64_t(1) << hb);
+    *pbits = table <= 64.0 * (1 << 20) ? 0 : (hb + 2 < 29 ? hb + 2 : 29);
+    if (*pbits != 0 && *pbits < hb) *pbits = hb;
     return RQ_OK;
 }
 
@@ -275,9 +306,12 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     cudaStream_t st = as_stream(stream);
     int *flag = scratch_err(scratch);
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
+    if (sub->lookup == RQ_LOOKUP_HASH && sub->pbits != 0 &&
+        (!sub->pmap || sub->pbits < 5 || sub->pbits > 32 || sub->pbits < sub->hbits))
+        return fail(RQ_E_ARG, "rq_subspace_build: presence bitmap missing or pbits out of range");
     const int rc = build_key_table(sub->states, D, sub->key_bits, sub->lookup == RQ_LOOKUP_HASH,
                                    sub->hkeys, sub->hvals, sub->hbits, &sub->empty_key, flag, gap,
-                                   st);
+                                   st, sub->pbits ? sub->pmap : nullptr, sub->pbits);
     if (rc != RQ_OK) return fail(rc, std::string("rq_subspace_build: ") + rq_last_error());
     RQ_CUDA(cudaMemsetAsync(sub->fbits, 0, RQ_FILTER_WORDS * sizeof(uint32_t), st));
     k_filter_build<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->fmask_a, sub->fmask_b,

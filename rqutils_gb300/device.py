@@ -62,7 +62,9 @@ class DeviceSubspace:
     """Sorted distinct states (uint64, bit q = qubit q) with their lookup structures."""
 
     def __init__(self, states, num_qubits=64, lookup='hash', filter_masks=None, device=None,
-                 stream=None, key_bits=None):
+                 stream=None, key_bits=None, presence=None):
+        """``presence``: None = a presence bitmap when the hash table does not fit in L2
+        (rq_presence_bits), False = none, an int = its size log2."""
         self.device = device or default_device()
         if isinstance(states, torch.Tensor):
             self.states = states.to(self.device, dtype=torch.int64).contiguous()
@@ -90,11 +92,23 @@ class DeviceSubspace:
         else:
             self.hkeys = self.hvals = None
         self.fbits = torch.zeros(L.FILTER_WORDS, dtype=torch.int32, device=self.device)
+        # presence bitmap in front of a hash table too large for L2
+        self.pbits = 0
+        self.pmap = None
+        if self.lookup == L.LOOKUP_HASH and presence is not False:
+            pb = ctypes.c_int32()
+            L.check(L.lib().rq_presence_bits(self.D, key_bits, ctypes.byref(pb)),
+                    'rq_presence_bits')
+            self.pbits = pb.value if presence is None else int(presence)
+            if self.pbits:
+                self.pmap = torch.empty((1 << self.pbits) // 32, dtype=torch.int32,
+                                        device=self.device)
         fa, fb = filter_masks if filter_masks is not None else default_filter_masks(num_qubits)
         self.scratch = scratch_tensor(self.D, self.device)
         self.c = L.Subspace(states=L.ptr(self.states), D=self.D, hkeys=L.ptr(self.hkeys),
                             hvals=L.ptr(self.hvals), hbits=self.hbits, lookup=self.lookup,
-                            key_bits=key_bits, empty_key=0, fmask_a=int(fa), fmask_b=int(fb), fbits=L.ptr(self.fbits))
+                            key_bits=key_bits, pbits=self.pbits, empty_key=0, fmask_a=int(fa),
+                            fmask_b=int(fb), fbits=L.ptr(self.fbits), pmap=L.ptr(self.pmap))
         L.check(L.lib().rq_subspace_build(ctypes.byref(self.c), L.ptr(self.scratch),
                                           L.stream_ptr(stream)), 'rq_subspace_build')
 

@@ -36,7 +36,8 @@ def _params(D, vtype, maxiter, tol, tol_dim, variant, mixed, target_rel, switch_
                           mixed=int(bool(mixed)), tol=float(tol or 0.),
                           tol_dim=float(tol_dim or 0.), switch_rel=float(switch_rel),
                           target_rel=float(target_rel or 0.), refresh=int(refresh),
-                          use_graph=int(bool(use_graph)), jacobi=int(bool(jacobi)),
+                          use_graph=int(use_graph) if use_graph in (0, 1, 2) else 1,
+                          jacobi=int(bool(jacobi)),
                           guard=int(bool(guard)))
 
 

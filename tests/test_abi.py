@@ -55,6 +55,10 @@ def test_host_only_entry_points(libpath):
     assert (4 << hb.value) >= 8 * (1 << 20)
     n = ctypes.c_size_t()
     assert lib.rq_scratch_size(1 << 20, ctypes.byref(n)) == 0 and n.value > 0
+    pb = ctypes.c_int32()
+    assert lib.rq_presence_bits(1 << 20, 32, ctypes.byref(pb)) == 0 and pb.value == 0
+    assert lib.rq_presence_bits(1 << 26, 64, ctypes.byref(pb)) == 0 and pb.value == 29
+    assert lib.rq_presence_bits(1 << 22, 64, ctypes.byref(pb)) == 0 and pb.value == 25
     prm = L.LobpcgParams(maxiter=10, variant=0, vtype=L.C128, mixed=1)
     assert lib.rq_lobpcg_workspace_size(1000, ctypes.byref(prm), ctypes.byref(n)) == 0
     assert n.value >= 8 * 1000 * 24
@@ -64,12 +68,12 @@ def test_host_only_entry_points(libpath):
 
 def test_struct_layouts():
     from rqutils_gb300 import _lib as L
-    assert ctypes.sizeof(L.Subspace) == 80
+    assert ctypes.sizeof(L.Subspace) == 88
     assert ctypes.sizeof(L.Terms) == 56
-    assert ctypes.sizeof(L.Operator) == 80 + 56 + 8 + 40 + 8
+    assert ctypes.sizeof(L.Operator) == 88 + 56 + 8 + 40 + 8
     assert ctypes.sizeof(L.LobpcgParams) == 64
     assert ctypes.sizeof(L.LobpcgResult) == 48
-    assert ctypes.sizeof(L.Batch) == 200
+    assert ctypes.sizeof(L.Batch) == 208
     assert L.Batch.terms.offset == 80 and L.Batch.nnz.offset == 184
     assert ctypes.sizeof(L.Mlp) == 56
 

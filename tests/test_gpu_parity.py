@@ -249,3 +249,65 @@ def test_chemistry_64bit_matvec(chem40, cache_level, lookup):
     assert np.linalg.norm(y32 - ref) <= 1e-6 * np.linalg.norm(ref)
     got = prob.sub.xsource(h.xmask).cpu().numpy()
     np.testing.assert_array_equal(got, xs)
+
+
+@pytest.mark.parametrize('mode', ['free', 'conn'])
+def test_presence_bitmap_keeps_results(chem40, mode):
+    """A presence bitmap forced onto a small table (it is built automatically only for tables
+    that do not fit in L2) changes no product and no connectivity list."""
+    import torch
+    from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    labels, coeffs, S, v, ref, xs = chem40
+    h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
+    terms = DeviceTerms(h)
+    plain = DeviceSubspace(S, num_qubits=h.num_qubits, presence=False)
+    assert plain.pbits == 0
+    withp = DeviceSubspace(S, num_qubits=h.num_qubits, presence=plain.hbits + 2)
+    assert withp.pbits == plain.hbits + 2
+    words = withp.pmap.cpu().numpy().view(np.uint32)
+    assert 0 < int(np.bitwise_count(words).sum()) <= len(S)
+    x = torch.as_tensor(v).cuda()
+    a = DeviceOperator(terms, plain, mode=mode)
+    b = DeviceOperator(terms, withp, mode=mode)
+    ya, yb = a.matvec(x), b.matvec(x)
+    b.check_errors()
+    assert torch.equal(ya, yb)
+    assert np.linalg.norm(yb.cpu().numpy() - ref) <= 1e-12 * np.linalg.norm(ref)
+    if mode == 'conn':
+        for u, w in zip(a.connectivity(), b.connectivity()):
+            np.testing.assert_array_equal(u, w)
+
+
+def test_presence_bitmap_batched():
+    import torch
+    from rqutils_gb300.batch import BatchedSQD
+    from rqutils_gb300.workloads import batched_random_problems
+    hams, states, ns = batched_random_problems(17, P=6, d_range=(200, 3000), k_range=(50, 200))
+    a = BatchedSQD(hams, states, presence=False)
+    b = BatchedSQD(hams, states, presence=int(a.c.hbits) + 2)
+    assert b.pbits > 0
+    rng = np.random.default_rng(1)
+    x = torch.as_tensor(rng.normal(size=a.D) + 1j * rng.normal(size=a.D)).cuda()
+    assert torch.equal(a.matvec(x), b.matvec(x))
+    b.check_errors()
+
+
+@pytest.mark.parametrize('cache_level', [(1, 0), (1, 2)])
+@pytest.mark.parametrize('variant', ['reference', 'fast'])
+def test_persistent_loop_matches_graph_loop(cache_level, variant):
+    """The persistent cooperative kernel (cached-connectivity / CSR operators) and the CUDA-graph
+    chunks run the same iteration: same eigenpair, iteration counts within one."""
+    import torch
+    from rqutils_gb300.ground_locg import lobpcg_solve
+    case = load('n16dense')
+    prob, h, S = _problem(case, cache_level=cache_level)
+    rng = np.random.default_rng(4)
+    x0 = torch.as_tensor(rng.normal(size=prob.sub.D)).to(prob.dtype).cuda()
+    for mixed in (False, True):
+        e1, x1, i1 = lobpcg_solve(prob.op, x0, variant=variant, mixed=mixed, use_graph=1)
+        e2, x2, i2 = lobpcg_solve(prob.op, x0, variant=variant, mixed=mixed, use_graph=2)
+        assert abs(e1 - e2) <= 1e-12 * abs(e2)
+        assert abs(i1['niter'] - i2['niter']) <= 1, (i1, i2)
+        assert i1['converged'] and i2['converged']
+        assert abs(torch.vdot(x1, x2).item()) > 1 - 1e-10
