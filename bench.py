@@ -586,6 +586,71 @@ def run_warmstart(args):
     print(json.dumps({'warmstart': ws}), flush=True)
 
 
+def run_svsim(args, rank, ws):
+    """State-vector simulation: a seeded random circuit of 200 Pauli-rotation gates (x, y, z, rx,
+    ry, rz, rzz on random qubits) on 30 qubits (2^30 complex128 amplitudes, 16 GiB) from |0>.
+    A step is the whole circuit; value = gates per second."""
+    import torch
+    from rqutils_gb300.svsim import apply_circuit, to_circuitxz
+    n, ngates = 30, 200
+    rng = np.random.default_rng(30)
+    names = ['x', 'y', 'z', 'rx', 'ry', 'rz', 'rzz']
+    circ = []
+    for _ in range(ngates):
+        nm = names[rng.integers(len(names))]
+        if nm == 'rzz':
+            circ.append((nm, rng.choice(n, size=2, replace=False), rng.uniform(-np.pi, np.pi)))
+        elif nm.startswith('r'):
+            circ.append((nm, int(rng.integers(n)), rng.uniform(-np.pi, np.pi)))
+        else:
+            circ.append((nm, int(rng.integers(n))))
+    cx = to_circuitxz(circ)
+    cx.num_qubits = n
+    nondiag = int(np.count_nonzero(cx.x))
+    runs = 0
+    prev_diag = False
+    for xv in cx.x:
+        d = xv == 0
+        if d and not prev_diag:
+            runs += 1
+        prev_diag = d
+    dev = torch.device('cuda', torch.cuda.current_device())
+    state = torch.zeros(1 << n, dtype=torch.complex128, device=dev)
+    state[0] = 1
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        apply_circuit(cx, state)
+    torch.cuda.synchronize()
+    times = time_steps(lambda: apply_circuit(cx, state), args.steps, lambda: None, stream)
+    t = sum(times) / 1e3 / args.steps
+    passes = nondiag + runs
+    abytes = passes * 2 * 16 * (1 << n)  # every pass reads and writes the state
+    peak, kind = measured_peaks()
+    # CPU: the oracle's restatement on a 2^22-amplitude state, scaled by amplitudes
+    from oracle import svsim as osv
+    nc = 22
+    cxc = to_circuitxz([(g[0], np.asarray(g[1]) % nc) + ((g[2],) if len(g) > 2 else ())
+                        for g in circ[:40]])
+    t0 = time.perf_counter()
+    osv.svsim(cxc.x, cxc.z, cxc.cos, cxc.sin, nc, 0)
+    tc = (time.perf_counter() - t0) / 40 * (1 << (n - nc))  # seconds per gate at n qubits
+    line = {'metric': 'svsim gates/s (30 qubits, complex128)', 'value': ngates / t, 'unit': 'gates/s',
+            'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * t,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128',
+            'data': 'synthetic',
+            'config': {'workload': 'svsim30_random200', 'num_qubits': n, 'gates': ngates,
+                       'non_diagonal_gates': nondiag, 'diagonal_runs': runs,
+                       'note': 'the circuit is applied in place to the resident state; the '
+                               '16 GiB state is far larger than L2'},
+            'roofline': {'bound': 'hbm', 'achieved': abytes / t / 1e9, 'peak': peak, 'unit': 'GB/s',
+                         'frac': abytes / t / 1e9 / peak, 'peak_source': f'{kind} hbm_gbs',
+                         'algorithmic_bytes_per_step': abytes},
+            'cpu_baseline': {'value': 1.0 / tc, 'unit': 'gates/s', 'cores': 1, 'kind': 'port',
+                             'sample': f'40 gates on {nc} qubits with the NumPy restatement, '
+                                       f'scaled by 2^{n - nc} amplitudes'}}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     """Only the timed loop of the headline (warm-up, then flush + matvec per step): the command
     that the ncu launch list and the kernel capture are taken on."""
@@ -794,7 +859,7 @@ def main():
     ap.add_argument('--rows', type=int, default=None,
                     help='override the subspace dimension (profiling captures on a small case)')
     ap.add_argument('--workload', default='hubbard',
-                    choices=['hubbard', 'chemistry', 'random20', 'batched', 'warmstart'],
+                    choices=['hubbard', 'chemistry', 'random20', 'batched', 'warmstart', 'svsim'],
                     help='hubbard: Hubbard 4x4, D=2^20 (the headline); chemistry: 64 qubits, '
                          '50,000 terms, D=2^26; random20: 20 qubits, 200 terms, D=16384; '
                          'batched: 256 random problems of 16..40 qubits in one launch')
@@ -816,6 +881,8 @@ def main():
     rank, ws = dist_init()
     if args.workload == 'batched':
         run_batched(args, rank, ws)
+    elif args.workload == 'svsim':
+        run_svsim(args, rank, ws)
     else:
         run_ours(args, rank, ws)
     if ws > 1:

@@ -165,13 +165,14 @@ struct SegOne {
 struct SegBatch {
     State *states;
     const int32_t *cprob;
-    const int64_t *crow;
+    const int64_t *crow;    // first row of each chunk
+    const int64_t *cend;    // one past the last row of each chunk
     const int32_t *cofs;
     double2 *part;          // [nchunks * kMaxReduce]
     unsigned int *counter;  // [P]
     __device__ __forceinline__ State *state() const { return states + cprob[blockIdx.x]; }
     __device__ __forceinline__ int64_t begin() const { return crow[blockIdx.x] + threadIdx.x; }
-    __device__ __forceinline__ int64_t end() const { return crow[blockIdx.x + 1]; }
+    __device__ __forceinline__ int64_t end() const { return cend[blockIdx.x]; }
     __device__ __forceinline__ int64_t stride() const { return blockDim.x; }
     template <int NV>
     __device__ void reduce(cdf (&v)[NV], int slot) const {
@@ -891,6 +892,10 @@ struct Phase {
     // connectivity or CSR operator of this phase's value type)
     const rq_operator_t *pop = nullptr;
     GridBar *bar = nullptr;
+    // optional: shrink the block list to the problems still active (active > 0) or restore the
+    // full list (active < 0); sets `grid`
+    int (*compact)(void *ctx, int active, int *grid, cudaStream_t s) = nullptr;
+    void *compact_ctx = nullptr;
 
     int pgrid() const { return (P + 127) / 128; }
 
@@ -1004,26 +1009,43 @@ int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s) {
         }
         return RQ_OK;
     }
-    cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    RQ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_chunk(s);
-    cudaError_t e = cudaStreamEndCapture(s, &graph);
-    if (rc != RQ_OK) {
-        if (graph) cudaGraphDestroy(graph);
-        return rc;
-    }
-    RQ_CUDA(e);
-    e = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    RQ_CUDA(e);
+    auto capture = [&]() -> int {
+        cudaGraph_t graph = nullptr;
+        RQ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_chunk(s);
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (rc != RQ_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        RQ_CUDA(e);
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        RQ_CUDA(e);
+        return RQ_OK;
+    };
+    RQ_TRY(capture());
+    int rc = RQ_OK;
+    cudaError_t e = cudaSuccess;
+    int last = ph.P;  // active problems when the block list was last rebuilt
     while (true) {
         e = cudaGraphLaunch(exec, s);
         if (e != cudaSuccess) break;
         rc = read_active(ph.nactive, active, s);
         if (rc != RQ_OK || active <= 0) break;
+        if (ph.compact && active * 4 <= last) {
+            // most problems have converged: launch blocks for the remaining ones only
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            rc = ph.compact(ph.compact_ctx, active, &ph.grid, s);
+            if (rc == RQ_OK) rc = capture();
+            if (rc != RQ_OK) break;
+            last = active;
+        }
     }
-    cudaGraphExecDestroy(exec);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (ph.compact && last != ph.P && rc == RQ_OK) rc = ph.compact(ph.compact_ctx, -1, &ph.grid, s);
     RQ_CUDA(e);
     return rc;
 }
@@ -1584,8 +1606,8 @@ struct MvBatch {
 struct BatchPlan {
     std::vector<int64_t> prow;
     std::vector<int32_t> cprob, cofs;
-    std::vector<int64_t> crow;
-    size_t states, err, part, counter, tcprob, tcrow, tcofs, vec_hi, vec_lo, total;
+    std::vector<int64_t> crow, cend;
+    size_t states, err, part, counter, tcprob, tcrow, tcend, tcofs, vec_hi, vec_lo, total;
     size_t hi_bytes, lo_bytes;
 };
 
@@ -1601,6 +1623,7 @@ int plan_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, BatchPlan &pl) 
         for (int64_t r = a; r < e; r += kBatchChunk) {
             pl.cprob.push_back(q);
             pl.crow.push_back(r);
+            pl.cend.push_back(std::min(r + kBatchChunk, e));
         }
         pl.cofs.push_back((int32_t)pl.cprob.size());
     }
@@ -1618,12 +1641,58 @@ int plan_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, BatchPlan &pl) 
     pl.counter = take(sizeof(unsigned int) * P);
     pl.tcprob = take(sizeof(int32_t) * nch);
     pl.tcrow = take(sizeof(int64_t) * (nch + 1));
+    pl.tcend = take(sizeof(int64_t) * nch);
     pl.tcofs = take(sizeof(int32_t) * (P + 1));
     pl.hi_bytes = (size_t)b.D * vtype_size(p.vtype);
     pl.lo_bytes = (size_t)b.D * vtype_size(lo_type(p.vtype));
     pl.vec_hi = take(8 * ((pl.hi_bytes + 255) & ~size_t(255)));
     pl.vec_lo = p.mixed ? take(8 * ((pl.lo_bytes + 255) & ~size_t(255))) : 0;
     pl.total = off;
+    return RQ_OK;
+}
+
+// Block lists of a batched solve: the full one, or the chunks of the problems still active.
+struct BatchBlocks {
+    const BatchPlan *pl;
+    int P;
+    State *states;
+    int32_t *cprob;
+    int64_t *crow, *cend;
+    int32_t *cofs;
+};
+
+int batch_compact(void *vctx, int active, int *grid, cudaStream_t s) {
+    BatchBlocks &c = *static_cast<BatchBlocks *>(vctx);
+    const BatchPlan &pl = *c.pl;
+    std::vector<int32_t> cprob, cofs(1, 0);
+    std::vector<int64_t> crow, cend;
+    if (active < 0) {  // restore
+        cprob = pl.cprob;
+        crow.assign(pl.crow.begin(), pl.crow.end() - 1);
+        cend = pl.cend;
+        cofs = pl.cofs;
+    } else {
+        std::vector<State> h(c.P);
+        RQ_CUDA(cudaMemcpyAsync(h.data(), c.states, sizeof(State) * c.P, cudaMemcpyDeviceToHost, s));
+        RQ_CUDA(cudaStreamSynchronize(s));
+        for (int q = 0; q < c.P; ++q) {
+            if (h[q].active)
+                for (int k = pl.cofs[q]; k < pl.cofs[q + 1]; ++k) {
+                    cprob.push_back(pl.cprob[k]);
+                    crow.push_back(pl.crow[k]);
+                    cend.push_back(pl.cend[k]);
+                }
+            cofs.push_back((int32_t)cprob.size());
+        }
+        if (cprob.empty()) return RQ_OK;  // nothing left: keep the list (every block returns)
+    }
+    const size_t n = cprob.size();
+    RQ_CUDA(cudaMemcpyAsync(c.cprob, cprob.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(c.crow, crow.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(c.cend, cend.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(c.cofs, cofs.data(), sizeof(int32_t) * cofs.size(), cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaStreamSynchronize(s));  // host vectors are temporaries
+    *grid = (int)n;
     return RQ_OK;
 }
 
@@ -1636,6 +1705,7 @@ int solve_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, const BatchPla
     unsigned int *counter = reinterpret_cast<unsigned int *>(ws + pl.counter);
     int32_t *cprob = reinterpret_cast<int32_t *>(ws + pl.tcprob);
     int64_t *crow = reinterpret_cast<int64_t *>(ws + pl.tcrow);
+    int64_t *cend = reinterpret_cast<int64_t *>(ws + pl.tcend);
     int32_t *cofs = reinterpret_cast<int32_t *>(ws + pl.tcofs);
     RQ_CUDA(cudaMemsetAsync(ws + pl.err, 0, 16, s));
     RQ_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int) * P, s));
@@ -1644,6 +1714,8 @@ int solve_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, const BatchPla
     RQ_CUDA(cudaMemcpyAsync(crow, pl.crow.data(), sizeof(int64_t) * pl.crow.size(),
                             cudaMemcpyHostToDevice, s));
     RQ_CUDA(cudaMemcpyAsync(cofs, pl.cofs.data(), sizeof(int32_t) * pl.cofs.size(),
+                            cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaMemcpyAsync(cend, pl.cend.data(), sizeof(int64_t) * pl.cend.size(),
                             cudaMemcpyHostToDevice, s));
     std::vector<double> tol_dim(P);
     for (int q = 0; q < P; ++q) {
@@ -1656,7 +1728,7 @@ int solve_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, const BatchPla
     const double tol = p.tol > 0 ? p.tol : eps_of(hi_type);
     const bool mixed = p.mixed && lo_type(hi_type) != hi_type;
     const int grid = (int)pl.cprob.size();
-    SegBatch seg{states, cprob, crow, cofs, reinterpret_cast<double2 *>(ws + pl.part), counter};
+    SegBatch seg{states, cprob, crow, cend, cofs, reinterpret_cast<double2 *>(ws + pl.part), counter};
     void *mvscratch = ws + pl.err - kScratchErr;
     const bool jac = p.jacobi != 0;
     Phase<VHI, SegBatch, MvBatch> hi{MvBatch{&b, mvscratch}, hi_type, seg, grid, states, P, nactive,
@@ -1665,6 +1737,9 @@ int solve_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, const BatchPla
                                      nactive,
                                      carve_vecs<VLO>(ws + (mixed ? pl.vec_lo : pl.vec_hi), pl.lo_bytes),
                                      jac, b.diag0};
+    BatchBlocks blocks{&pl, P, states, cprob, crow, cend, cofs};
+    hi.compact = lo.compact = batch_compact;
+    hi.compact_ctx = lo.compact_ctx = &blocks;
     std::vector<int> nlo;
     RQ_TRY(run_phases(lo, hi, mixed, p, tol, tol_dim, b.D, x0, pl.hi_bytes, kChunk,
                       p.use_graph != 0, s, nlo));

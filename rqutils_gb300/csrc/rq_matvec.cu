@@ -256,6 +256,7 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
                     if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
                     b[u] = hs ^ hxg;
                 }
+
                 if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
                     uint32_t pw[U];
 #pragma unroll

@@ -6,7 +6,7 @@
 // A non-diagonal gate is one in-place pass over the pairs (i, i ^ x): each thread reads both
 // amplitudes of its pair and writes both outputs.  Products and sums are rounded one at a time
 // (no fused multiply-add) in the order of the reference's complex arithmetic, so results equal
-// the reference arithmetic bit for bit.
+// the reference arithmetic bit for bit (up to the sign of zero results).
 #include <vector>
 
 #include "rq_common.cuh"
@@ -20,12 +20,13 @@ struct Gate {
     double c, s;
 };
 
-// out = i s sigma v_src + c v_self   (sigma = +-1)
-__device__ __forceinline__ double2 rot(double c, double s, double sigma, double2 self, double2 src, bool with_c) {
-    const double a = __dmul_rn(s, sigma);
-    // (0 + i a)(re + i im) = (0 re - a im) + i (0 im + a re)
-    double re = __dsub_rn(__dmul_rn(0.0, src.x), __dmul_rn(a, src.y));
-    double im = __dadd_rn(__dmul_rn(0.0, src.y), __dmul_rn(a, src.x));
+// out = i s sigma v_src + c v_self   (sigma = +-1).  (0 + i a)(re + i im) = (0 re - a im) +
+// i (0 im + a re); the 0 x terms only decide the sign of a zero result and are left out
+// (GB300 issues FP64 at a small fraction of its FP32 rate), as is the product s sigma (exact).
+__device__ __forceinline__ double2 rot(double c, double s, bool neg, double2 self, double2 src, bool with_c) {
+    const double a = neg ? -s : s;
+    double re = -__dmul_rn(a, src.y);
+    double im = __dmul_rn(a, src.x);
     if (with_c) {
         re = __dadd_rn(re, __dmul_rn(c, self.x));
         im = __dadd_rn(im, __dmul_rn(c, self.y));
@@ -33,9 +34,7 @@ __device__ __forceinline__ double2 rot(double c, double s, double sigma, double2
     return make_double2(re, im);
 }
 
-__device__ __forceinline__ double parity_sign(uint64_t i, uint64_t z) {
-    return (__popcll(i & z) & 1) ? -1.0 : 1.0;
-}
+__device__ __forceinline__ bool parity_odd(uint64_t i, uint64_t z) { return __popcll(i & z) & 1; }
 
 // gates [g0, g1) are diagonal
 __global__ void k_diag_run(double2 *__restrict__ psi, uint64_t N, const Gate *__restrict__ gates, int g0, int g1) {
@@ -43,7 +42,7 @@ __global__ void k_diag_run(double2 *__restrict__ psi, uint64_t N, const Gate *__
         double2 v = psi[i];
         for (int g = g0; g < g1; ++g) {
             const Gate G = gates[g];
-            v = rot(G.c, G.s, parity_sign(i, G.z), v, v, G.c != 0.0);
+            v = rot(G.c, G.s, parity_odd(i, G.z), v, v, G.c != 0.0);
         }
         psi[i] = v;
     }
@@ -59,8 +58,8 @@ __global__ void k_pair(double2 *__restrict__ psi, uint64_t N, const Gate *__rest
         const uint64_t j = i ^ G.x;
         const double2 a = psi[i], b = psi[j];
         const bool wc = G.c != 0.0;
-        psi[i] = rot(G.c, G.s, parity_sign(i, G.z), a, b, wc);
-        psi[j] = rot(G.c, G.s, parity_sign(j, G.z), b, a, wc);
+        psi[i] = rot(G.c, G.s, parity_odd(i, G.z), a, b, wc);
+        psi[j] = rot(G.c, G.s, parity_odd(j, G.z), b, a, wc);
     }
 }
 

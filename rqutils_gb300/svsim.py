@@ -111,6 +111,17 @@ def svsim(circuit, initial_state=0, out_sharding=None, *, device=None, stream=No
         state = torch.as_tensor(np.asarray(initial_state, dtype=np.complex128)).to(dev)
     if state.numel() != N:
         raise ValueError(f'initial state has {state.numel()} amplitudes for {n} qubits')
+    return apply_circuit(circ, state, stream=stream)
+
+
+def apply_circuit(circuit, state, stream=None):
+    """Apply the circuit to a complex128 device state of 2^num_qubits amplitudes in place."""
+    circ = to_circuitxz(circuit)
+    n = int(circ.num_qubits)
+    if state.dtype != torch.complex128 or not state.is_cuda or state.numel() != (1 << n):
+        raise ValueError('state must be a complex128 CUDA tensor of 2^num_qubits amplitudes')
+    state = state.contiguous() if not state.is_contiguous() else state
+    dev = state.device
     ng = len(circ.x)
     x = np.ascontiguousarray(circ.x, dtype=np.int64)
     z = np.ascontiguousarray(circ.z, dtype=np.int64)
