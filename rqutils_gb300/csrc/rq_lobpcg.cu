@@ -111,7 +111,10 @@ struct CDot {
         }
     }
     __device__ __forceinline__ double2 get() const { return make_double2(re.get(), im.get()); }
-    __device__ __forceinline__ cdf get_cdf() const { return {re.get_df(), im.get_df()}; }
+    // real vectors leave im at zero: no conversion for it
+    __device__ __forceinline__ cdf get_cdf(bool cplx = true) const {
+        return {re.get_df(), cplx ? im.get_df() : df{0.f, 0.f}};
+    }
 };
 
 template <typename R>
@@ -242,7 +245,7 @@ __device__ __forceinline__ void d_dots(SEG seg, Pairs<V, NP> pr, int slot) {
     }
     cdf v[NP];
 #pragma unroll
-    for (int k = 0; k < NP; ++k) v[k] = acc[k].get_cdf();
+    for (int k = 0; k < NP; ++k) v[k] = acc[k].get_cdf(VT<V>::kComplex);
     seg.template reduce<NP>(v, slot);
 }
 template <typename V, int NP, typename SEG>
@@ -288,7 +291,7 @@ __device__ __forceinline__ void d_sub2_norm(SEG seg, const V *x, const V *y, V *
         VT<V>::st(v, i, w);
         nn.add(w, w, VT<V>::kComplex);
     }
-    cdf r[1] = {nn.get_cdf()};
+    cdf r[1] = {nn.get_cdf(VT<V>::kComplex)};
     seg.template reduce<1>(r, kVn);
 }
 template <typename V, typename SEG>
@@ -316,7 +319,7 @@ __device__ __forceinline__ void d_scale_dots2(SEG seg, const V *x, const V *y, V
         d0.add(VT<V>::ld(x, i), w, VT<V>::kComplex);
         d1.add(VT<V>::ld(y, i), w, VT<V>::kComplex);
     }
-    cdf r[2] = {d0.get_cdf(), d1.get_cdf()};
+    cdf r[2] = {d0.get_cdf(VT<V>::kComplex), d1.get_cdf(VT<V>::kComplex)};
     seg.template reduce<2>(r, kIp0);
 }
 template <typename V, typename SEG>
@@ -365,7 +368,7 @@ __device__ __forceinline__ void d_gram3(SEG seg, const V *x, const V *y, const V
     }
     cdf r[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) r[k] = g[k].get_cdf();
+    for (int k = 0; k < 6; ++k) r[k] = g[k].get_cdf(VT<V>::kComplex);
     seg.template reduce<6>(r, kG10);
 }
 template <typename V, typename SEG>
@@ -390,7 +393,7 @@ __device__ __forceinline__ void d_gram2(SEG seg, const V *x, const V *p, const V
         g[1].add(xi, axi, c);
         g[2].add(pi, api, c);
     }
-    cdf r[3] = {g[0].get_cdf(), g[1].get_cdf(), g[2].get_cdf()};
+    cdf r[3] = {g[0].get_cdf(VT<V>::kComplex), g[1].get_cdf(VT<V>::kComplex), g[2].get_cdf(VT<V>::kComplex)};
     seg.template reduce<3>(r, kG10);
 }
 template <typename V, typename SEG>
@@ -411,7 +414,7 @@ __device__ __forceinline__ void d_upd_s(SEG seg, const V *y, const V *p) {
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
         nn.add(s, s, VT<V>::kComplex);
     }
-    cdf r[1] = {nn.get_cdf()};
+    cdf r[1] = {nn.get_cdf(VT<V>::kComplex)};
     seg.template reduce<1>(r, kSn);
 }
 template <typename V, typename SEG>
@@ -446,7 +449,7 @@ __device__ __forceinline__ void d_upd_tu(SEG seg, const V *x, const V *y, const 
         tn.add(t, t, VT<V>::kComplex);
         un.add(u, u, VT<V>::kComplex);
     }
-    cdf r[2] = {tn.get_cdf(), un.get_cdf()};
+    cdf r[2] = {tn.get_cdf(VT<V>::kComplex), un.get_cdf(VT<V>::kComplex)};
     seg.template reduce<2>(r, kTn);
 }
 template <typename V, typename SEG>
@@ -516,7 +519,7 @@ __device__ __forceinline__ void d_upd2_norms(SEG seg, const V *x, const V *p) {
         tn.add(t, t, VT<V>::kComplex);
         un.add(u, u, VT<V>::kComplex);
     }
-    cdf r[2] = {tn.get_cdf(), un.get_cdf()};
+    cdf r[2] = {tn.get_cdf(VT<V>::kComplex), un.get_cdf(VT<V>::kComplex)};
     seg.template reduce<2>(r, kTn);
 }
 template <typename V, typename SEG>
@@ -564,7 +567,7 @@ __device__ __forceinline__ void d_resid(SEG seg, const V *ax, const V *x, V *r, 
         an.add(a, a, VT<V>::kComplex);
         rn.add(w, w, VT<V>::kComplex);
     }
-    cdf out[2] = {an.get_cdf(), rn.get_cdf()};
+    cdf out[2] = {an.get_cdf(VT<V>::kComplex), rn.get_cdf(VT<V>::kComplex)};
     seg.template reduce<2>(out, kAxn);
 }
 template <typename V, typename SEG>
@@ -1258,6 +1261,8 @@ int run_persist(PH &ph, int variant, cudaStream_t s) {
     int per = 0;
     RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, 0));
     if (per < 1) return run_loop(ph, variant, true, kChunk, s);
+    // as many blocks as the phase's kernels use, within the co-resident limit (the element-wise
+    // FP64 work needs every SM; fewer, longer threads measured slower at D = 2^16)
     int grid = ph.grid;
     if (grid > per * sm_count()) grid = per * sm_count();
     if (grid > kMaxReduceBlocks / 2) grid = kMaxReduceBlocks / 2;  // two halves of partial sums
