@@ -39,7 +39,14 @@ sys.path.insert(0, ROOT)
 METRIC = 'Pauli-matvec/s & time-to-residual 1e-8 (learned warm-start vs plain), 1 GB300'
 UNIT = 'matvec/s'
 L2_FLUSH_BYTES = 256 << 20
-PROFILE_TRAFFIC = os.path.join(ROOT, 'profiles', 'matvec_free_hubbard4x4_D1048576.txt')
+# ncu DRAM traffic of one launch of the headline kernel, per workload: (summary file, rows of the
+# captured launch); a capture on fewer rows is scaled by rows (the traffic is linear in rows)
+PROFILES = {
+    'hubbard': (os.path.join(ROOT, 'profiles', 'matvec_free_hubbard4x4_D1048576.txt'), 1 << 20),
+    'chemistry': (os.path.join(ROOT, 'profiles', 'matvec_free_chemistry64_K50000_rows4194304.txt'),
+                  1 << 22),
+    'batched': (os.path.join(ROOT, 'profiles', 'batch_matvec_free_random256.txt'), None),
+}
 
 
 class Workload:
@@ -192,12 +199,17 @@ def algorithmic_bytes(D, J, J0, hits, bv):
     return 8 * D + bv * D + bv * D + 8 * D * (J - J0) + bv * hits
 
 
-def read_profile_traffic():
+def read_profile_traffic(workload, rows=None):
+    """DRAM bytes of one launch from the committed ncu summary, scaled to `rows`."""
+    if workload not in PROFILES:
+        return None
+    path, prow = PROFILES[workload]
     try:
-        with open(PROFILE_TRAFFIC) as fh:
+        with open(path) as fh:
             for line in fh:
                 if line.startswith('dram_bytes_per_launch:'):
-                    return float(line.split(':', 1)[1])
+                    t = float(line.split(':', 1)[1])
+                    return t * rows / prow if (rows and prow) else t
     except OSError:
         pass
     return None
@@ -317,7 +329,7 @@ def run_ours(args, rank, ws):
     abytes = algorithmic_bytes(D, J, J0, hits, bv)
     peak, peak_kind = measured_peaks()
     achieved = abytes / (ms_per_step / 1e3) / 1e9
-    traffic = read_profile_traffic() if wl.name == 'hubbard' else None
+    traffic = read_profile_traffic(wl.name, D) if wl.name in ('hubbard', 'chemistry') else None
 
     lob = {}
     if wl.lobpcg:
@@ -511,7 +523,7 @@ def run_batched(args, rank, ws):
                 'h2d_bytes_per_step': bv * wl.D, 'd2h_bytes_per_step': bv * wl.D},
         'gpu_launches': args.steps,
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
-                     'frac': achieved / peak, 'traffic': None,
+                     'frac': achieved / peak, 'traffic': read_profile_traffic('batched'),
                      'peak_source': f'{peak_kind} hbm_gbs',
                      'algorithmic_bytes_per_launch': abytes},
         'modes': {'conn_problem_matvec_per_s': wl.P * 1e3 / t_conn,
