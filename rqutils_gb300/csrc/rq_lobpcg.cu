@@ -219,6 +219,16 @@ struct SegBatch {
     }                                 \
     __syncthreads();
 
+// The same for coefficients already converted to the pass's arithmetic type R (a double ->
+// float conversion also issues on the FP64 pipe).
+#define BLOCK_R(n, body)              \
+    __shared__ R br_[n];              \
+    if (threadIdx.x == 0) {           \
+        R *out = br_;                 \
+        body;                         \
+    }                                 \
+    __syncthreads();
+
 #define SEG_LOOP(i) for (int64_t i = seg.begin(); i < seg.end(); i += seg.stride())
 
 // ------------------------------------------------------------------------------------------
@@ -260,11 +270,11 @@ __device__ __forceinline__ void d_normalize(SEG seg, const V *in, V *out, int ns
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    BLOCK_SCALARS(1, {
+    BLOCK_R(1, {
         const double n = sqrt(st->red[nslot].x);
-        out[0] = n == 0. ? 1. : 1. / n;
+        out[0] = (R)(n == 0. ? 1. : 1. / n);
     })
-    const R inv = (R)bs_[0];
+    const R inv = br_[0];
     SEG_LOOP(i) {
         cx<R> v = VT<V>::ld(in, i);
         VT<V>::st(out, i, {v.re * inv, v.im * inv});
@@ -282,8 +292,13 @@ __device__ __forceinline__ void d_sub2_norm(SEG seg, const V *x, const V *y, V *
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const cx<R> m0 = c_of<R>(make_double2(-st->red[kIp0].x, -st->red[kIp0].y));
-    const cx<R> m1 = c_of<R>(make_double2(-st->red[kIp1].x, -st->red[kIp1].y));
+    BLOCK_R(4, {
+        out[0] = (R)(-st->red[kIp0].x);
+        out[1] = (R)(-st->red[kIp0].y);
+        out[2] = (R)(-st->red[kIp1].x);
+        out[3] = (R)(-st->red[kIp1].y);
+    })
+    const cx<R> m0 = {br_[0], br_[1]}, m1 = {br_[2], br_[3]};
     CDot<R> nn;
     SEG_LOOP(i) {
         cx<R> w = axpy(m0, VT<V>::ld(x, i), VT<V>::ld(v, i));
@@ -306,11 +321,11 @@ __device__ __forceinline__ void d_scale_dots2(SEG seg, const V *x, const V *y, V
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    BLOCK_SCALARS(1, {
+    BLOCK_R(1, {
         const double n = sqrt(st->red[kVn].x);
-        out[0] = (!do_scale || n == 0.) ? 1. : 1. / n;
+        out[0] = (R)((!do_scale || n == 0.) ? 1. : 1. / n);
     })
-    const R inv = (R)bs_[0];
+    const R inv = br_[0];
     CDot<R> d0, d1;
     SEG_LOOP(i) {
         cx<R> w = VT<V>::ld(v, i);
@@ -334,8 +349,8 @@ __device__ __forceinline__ void d_mask(SEG seg, const V *v, V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    BLOCK_SCALARS(1, { out[0] = sqrt(st->red[kVn].x) >= 0.99 ? 1. : 0.; })
-    const R m = (R)bs_[0];
+    BLOCK_R(1, { out[0] = (R)(sqrt(st->red[kVn].x) >= 0.99 ? 1. : 0.); })
+    const R m = br_[0];
     SEG_LOOP(i) {
         cx<R> w = VT<V>::ld(v, i);
         VT<V>::st(p, i, {w.re * m, w.im * m});
@@ -408,7 +423,13 @@ __device__ __forceinline__ void d_upd_s(SEG seg, const V *y, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const cx<R> k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
+    BLOCK_R(4, {
+        out[0] = (R)st->kappa[1].x;
+        out[1] = (R)st->kappa[1].y;
+        out[2] = (R)st->kappa[2].x;
+        out[3] = (R)st->kappa[2].y;
+    })
+    const cx<R> k1 = {br_[0], br_[1]}, k2 = {br_[2], br_[3]};
     CDot<R> nn;
     SEG_LOOP(i) {
         const cx<R> s = axpy(k2, VT<V>::ld(p, i), cmul(k1, VT<V>::ld(y, i)));
@@ -429,17 +450,23 @@ __device__ __forceinline__ void d_upd_tu(SEG seg, const V *x, const V *y, const 
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    BLOCK_SCALARS(3, {
+    BLOCK_R(10, {
         const double ns = sqrt(st->red[kSn].x);
-        out[0] = ns;
-        out[1] = st->kappa[0].x / ns;
-        out[2] = st->kappa[0].y / ns;
+        out[0] = (R)(-ns);
+        out[1] = (R)(st->kappa[0].x / ns);
+        out[2] = (R)(st->kappa[0].y / ns);
+        out[3] = (R)st->kappa[0].x;
+        out[4] = (R)st->kappa[0].y;
+        out[5] = (R)st->kappa[1].x;
+        out[6] = (R)st->kappa[1].y;
+        out[7] = (R)st->kappa[2].x;
+        out[8] = (R)st->kappa[2].y;
+        out[9] = (R)((st->guard && ns == 0.) ? 1 : 0);  // s = 0: y' = y instead of 0 * inf
     })
-    const double ns = bs_[0];
-    const bool keep_y = st->guard && ns == 0.;  // s = 0: y' = y instead of 0 * inf
-    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
-    const cx<R> k0s = c_of<R>(make_double2(bs_[1], bs_[2]));
-    const cx<R> mns = {(R)(-ns), (R)0};
+    const bool keep_y = br_[9] != (R)0;
+    const cx<R> k0 = {br_[3], br_[4]}, k1 = {br_[5], br_[6]}, k2 = {br_[7], br_[8]};
+    const cx<R> k0s = {br_[1], br_[2]};
+    const cx<R> mns = {br_[0], (R)0};
     CDot<R> tn, un;
     SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i);
@@ -464,20 +491,26 @@ __device__ __forceinline__ void d_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax,
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    BLOCK_SCALARS(5, {
+    BLOCK_R(12, {
         const double ns = sqrt(st->red[kSn].x);
-        out[0] = ns;
-        out[1] = st->kappa[0].x / ns;
-        out[2] = st->kappa[0].y / ns;
-        out[3] = 1. / sqrt(st->red[kTn].x);
-        out[4] = 1. / sqrt(st->red[kUn].x);
+        out[0] = (R)(-ns);
+        out[1] = (R)(st->kappa[0].x / ns);
+        out[2] = (R)(st->kappa[0].y / ns);
+        out[3] = (R)st->kappa[0].x;
+        out[4] = (R)st->kappa[0].y;
+        out[5] = (R)st->kappa[1].x;
+        out[6] = (R)st->kappa[1].y;
+        out[7] = (R)st->kappa[2].x;
+        out[8] = (R)st->kappa[2].y;
+        out[9] = (R)((st->guard && ns == 0.) ? 1 : 0);  // s = 0: y' = y instead of 0 * inf
+        out[10] = (R)(1. / sqrt(st->red[kTn].x));
+        out[11] = (R)(1. / sqrt(st->red[kUn].x));
     })
-    const double ns = bs_[0];
-    const bool keep_y = st->guard && ns == 0.;  // s = 0: y' = y instead of 0 * inf
-    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]), k2 = c_of<R>(st->kappa[2]);
-    const cx<R> k0s = c_of<R>(make_double2(bs_[1], bs_[2]));
-    const cx<R> mns = {(R)(-ns), (R)0};
-    const R rit = (R)bs_[3], riu = (R)bs_[4];
+    const bool keep_y = br_[9] != (R)0;
+    const cx<R> k0 = {br_[3], br_[4]}, k1 = {br_[5], br_[6]}, k2 = {br_[7], br_[8]};
+    const cx<R> k0s = {br_[1], br_[2]};
+    const cx<R> mns = {br_[0], (R)0};
+    const R rit = br_[10], riu = br_[11];
     SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i);
         const cx<R> yi = VT<V>::ld(y, i);
@@ -509,7 +542,13 @@ __device__ __forceinline__ void d_upd2_norms(SEG seg, const V *x, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]);
+    BLOCK_R(4, {
+        out[0] = (R)st->kappa[0].x;
+        out[1] = (R)st->kappa[0].y;
+        out[2] = (R)st->kappa[1].x;
+        out[3] = (R)st->kappa[1].y;
+    })
+    const cx<R> k0 = {br_[0], br_[1]}, k1 = {br_[2], br_[3]};
     const cx<R> mk1 = {-k1.re, -k1.im};
     CDot<R> tn, un;
     SEG_LOOP(i) {
@@ -533,9 +572,17 @@ __device__ __forceinline__ void d_upd2_xy(SEG seg, V *x, V *y, const V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const cx<R> k0 = c_of<R>(st->kappa[0]), k1 = c_of<R>(st->kappa[1]);
+    BLOCK_R(6, {
+        out[0] = (R)st->kappa[0].x;
+        out[1] = (R)st->kappa[0].y;
+        out[2] = (R)st->kappa[1].x;
+        out[3] = (R)st->kappa[1].y;
+        out[4] = (R)(1. / sqrt(st->red[kTn].x));
+        out[5] = (R)(1. / sqrt(st->red[kUn].x));
+    })
+    const cx<R> k0 = {br_[0], br_[1]}, k1 = {br_[2], br_[3]};
     const cx<R> mk1 = {-k1.re, -k1.im};
-    const R rit = (R)(1. / sqrt(st->red[kTn].x)), riu = (R)(1. / sqrt(st->red[kUn].x));
+    const R rit = br_[4], riu = br_[5];
     SEG_LOOP(i) {
         const cx<R> xi = VT<V>::ld(x, i), pi = VT<V>::ld(p, i);
         const cx<R> t = axpy(mk1, xi, cmul(k0, pi));
@@ -557,8 +604,8 @@ __device__ __forceinline__ void d_resid(SEG seg, const V *ax, const V *x, V *r, 
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const double th = use_rho ? st->red[kMisc].x : st->theta;
-    const cx<R> mth = {(R)(-th), (R)0};
+    BLOCK_R(1, { out[0] = (R)(-(use_rho ? st->red[kMisc].x : st->theta)); })
+    const cx<R> mth = {br_[0], (R)0};
     CDot<R> an, rn;
     SEG_LOOP(i) {
         const cx<R> a = VT<V>::ld(ax, i);
@@ -582,12 +629,21 @@ __device__ __forceinline__ void d_jacobi(SEG seg, const double *diag, const V *r
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    const double th = st->theta;
-    const double floor_ = 1e-8 * (1. + fabs(th));
+    // a preconditioner needs no FP64 quotient: the reciprocal is taken in FP32 (GB300's FP64
+    // division costs more than the rest of the pass)
+    __shared__ double th_s;
+    __shared__ float floor_s;
+    if (threadIdx.x == 0) {
+        th_s = st->theta;
+        floor_s = (float)(1e-8 * (1. + fabs(st->theta)));
+    }
+    __syncthreads();
+    const double th = th_s;
+    const float floor_ = floor_s;
     SEG_LOOP(i) {
-        double den = diag[i] - th;
-        if (fabs(den) < floor_) den = den < 0 ? -floor_ : floor_;
-        const R f = (R)(1. / den);
+        float den = (float)(diag[i] - th);
+        if (fabsf(den) < floor_) den = den < 0.f ? -floor_ : floor_;
+        const R f = (R)(1.f / den);
         const cx<R> v = VT<V>::ld(r, i);
         VT<V>::st(w, i, {v.re * f, v.im * f});
     }
@@ -1394,7 +1450,8 @@ int solve(const rq_operator_t &op, MV mv, bool callback, const rq_lobpcg_params_
                               jac, op.diag0};
     std::vector<int> nlo;
     const bool graph = p.use_graph != 0 && !callback;
-    if (graph && p.use_graph != 2 && (op.mode == RQ_MODE_CONN || op.mode == RQ_MODE_CSR)) {
+    // (the Jacobi preconditioner measured slower inside the persistent kernel: graphs then)
+    if (graph && p.use_graph != 2 && !jac && (op.mode == RQ_MODE_CONN || op.mode == RQ_MODE_CSR)) {
         // one persistent kernel per phase; CSR values must be of the phase's own type
         GridBar *bar = reinterpret_cast<GridBar *>(ws + L.err + 16);
         if (op.mode == RQ_MODE_CONN || op.val_vtype == hi_type) {
