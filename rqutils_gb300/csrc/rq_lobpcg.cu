@@ -362,6 +362,30 @@ k_mask(SEG seg, const V *v, V *p) {
     d_mask<V, SEG>(seg, v, p);
 }
 
+// FAST projection, last step: p = v / |v|, or 0 when |v| < thr |r| (r numerically inside the span
+// of x, y; the role of the 0.99 cut of ground_locg.py:421); |v|^2 in red[kVn], |r|^2 in red[kG10 + 5]
+template <typename V, typename SEG>
+__device__ __forceinline__ void d_norm_mask(SEG seg, const V *v, V *p) {
+    State *st = seg.state();
+    GATE(st);
+    using R = typename VT<V>::R;
+    BLOCK_R(1, {
+        const double n2 = st->red[kVn].x;
+        const double r2 = st->red[kG10 + 5].x;
+        const double thr = sizeof(R) == 4 ? 1e-5 : 1e-10;
+        out[0] = (R)((n2 > 0. && n2 > thr * thr * r2) ? 1. / sqrt(n2) : 0.);
+    })
+    const R m = br_[0];
+    SEG_LOOP(i) {
+        cx<R> w = VT<V>::ld(v, i);
+        VT<V>::st(p, i, {w.re * m, w.im * m});
+    }
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads) k_norm_mask(SEG seg, const V *v, V *p) {
+    d_norm_mask<V, SEG>(seg, v, p);
+}
+
 // Gram entries of (x, y, p): <y,Ax> <p,Ax> <p,Ay> <x,Ax> <y,Ay> <p,Ap>
 template <typename V, typename SEG>
 __device__ __forceinline__ void d_gram3(SEG seg, const V *x, const V *y, const V *p, const V *ax, const V *ay,
@@ -837,6 +861,29 @@ __global__ void k_check(State *states, int P, int *nactive) {
 }
 
 // FAST: a refresh starts -- reset the counter (runs only when want_refresh is set)
+// FAST projection: both rounds of classical Gram-Schmidt against (x, y) from one set of inner
+// products.  With c = (<x,r>, <y,r>) and G the Gram matrix of (x, y), the second round's
+// coefficients are c - G c, so r is projected once with e = 2 c - G c (slots kG10..: <x,r>, <y,r>,
+// <x,x>, <x,y>, <y,y>, <r,r>; e goes to kIp0, kIp1 for the subtraction pass).
+__device__ __forceinline__ void d_proj_coef(State *states, int P, int first, int step) {
+    FOR_ACTIVE_PROBLEMS(states, P, st) {
+        const double2 cx_ = st->red[kG10], cy = st->red[kG10 + 1];
+        const double2 gxx = st->red[kG10 + 2], gxy = st->red[kG10 + 3], gyy = st->red[kG10 + 4];
+        auto mul = [](double2 a, double2 b) {
+            return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        };
+        const double2 gyx = make_double2(gxy.x, -gxy.y);  // <y, x>
+        const double2 ax = mul(gxx, cx_), bx = mul(gxy, cy);
+        const double2 ay = mul(gyx, cx_), by = mul(gyy, cy);
+        st->red[kIp0] = make_double2(2. * cx_.x - ax.x - bx.x, 2. * cx_.y - ax.y - bx.y);
+        st->red[kIp1] = make_double2(2. * cy.x - ay.x - by.x, 2. * cy.y - ay.y - by.y);
+        break;
+    }
+}
+__global__ void k_proj_coef(State *states, int P) {
+    d_proj_coef(states, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 __device__ __forceinline__ void d_refresh_mark(State *states, int P, int first, int step) {
     FOR_ACTIVE_PROBLEMS(states, P, st) {
         if (st->want_refresh) {
@@ -963,7 +1010,15 @@ struct Phase {
     }
 
     // project_out((x, y), src) -> p  (ground_locg.py:380-421); src is overwritten
-    void project(V *src, cudaStream_t s) {
+    void project(V *src, cudaStream_t s, int variant = RQ_LOBPCG_REFERENCE) {
+        if (variant == RQ_LOBPCG_FAST) {
+            Pairs<V, 6> g{{v.x, v.y, v.x, v.x, v.y, src}, {src, src, v.x, v.y, v.y, src}};
+            k_dots<V, 6, SEG><<<grid, kThreads, 0, s>>>(seg, g, kG10);
+            k_proj_coef<<<pgrid(), 128, 0, s>>>(states, P);
+            k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
+            k_norm_mask<V, SEG><<<grid, kThreads, 0, s>>>(seg, src, v.p);
+            return;
+        }
         Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
         k_dots<V, 2, SEG><<<grid, kThreads, 0, s>>>(seg, pr, kIp0);
         k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
@@ -983,7 +1038,7 @@ struct Phase {
             k_jacobi<V, SEG><<<grid, kThreads, 0, s>>>(seg, diag, v.r, v.w);
             src = v.w;
         }
-        project(src, s);
+        project(src, s, variant);
         if (variant == RQ_LOBPCG_REFERENCE) {
             RQ_TRY(matvec(v.x, v.ax, s));
             RQ_TRY(matvec(v.y, v.ay, s));
@@ -1262,16 +1317,25 @@ __global__ void __launch_bounds__(kThreads) k_persist(const PersistArgs<V> a) {
             src = v.w;
         }
         // project_out((x, y), src) -> p
-        Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
-        d_dots<V, 2, SegPersist>(seg, pr, kIp0);
-        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-        d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
-        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-        d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
-        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-        d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 0);
-        d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-        d_mask<V, SegPersist>(seg, src, v.p);
+        if (a.variant == RQ_LOBPCG_FAST) {
+            Pairs<V, 6> g{{v.x, v.y, v.x, v.x, v.y, src}, {src, src, v.x, v.y, v.y, src}};
+            d_dots<V, 6, SegPersist>(seg, g, kG10);
+            if (threadIdx.x == 0) d_proj_coef(st, 1, 0, kOnce);
+            scalar_done();
+            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+            d_norm_mask<V, SegPersist>(seg, src, v.p);
+        } else {
+            Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
+            d_dots<V, 2, SegPersist>(seg, pr, kIp0);
+            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+            d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
+            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+            d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
+            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+            d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 0);
+            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
+            d_mask<V, SegPersist>(seg, src, v.p);
+        }
         if (!sync()) break;  // the products gather p (and x, y) from every block's rows
         if (a.variant == RQ_LOBPCG_REFERENCE) {
             persist_mv<V, MVK>(a, st, v.x, v.ax, nullptr);
