@@ -509,6 +509,38 @@ k_upd_tu(SEG seg, const V *x, const V *y, const V *p) {
     d_upd_tu<V, SEG>(seg, x, y, p);
 }
 
+// FAST: s = k1 y + k2 p once, with <s,s>, <x,s>, <x,x>, <y,y> into kG10..kG10+3 (the norms of
+// t = s k0/|s| - x |s| and u = k0 x + s follow from them, d_stu_coef), one reduction instead of two
+template <typename V, typename SEG>
+__device__ __forceinline__ void d_upd_stu(SEG seg, const V *x, const V *y, const V *p) {
+    State *st = seg.state();
+    GATE(st);
+    using R = typename VT<V>::R;
+    BLOCK_R(4, {
+        out[0] = (R)st->kappa[1].x;
+        out[1] = (R)st->kappa[1].y;
+        out[2] = (R)st->kappa[2].x;
+        out[3] = (R)st->kappa[2].y;
+    })
+    const cx<R> k1 = {br_[0], br_[1]}, k2 = {br_[2], br_[3]};
+    CDot<R> ss, xs, xx, yy;
+    SEG_LOOP(i) {
+        const cx<R> xi = VT<V>::ld(x, i), yi = VT<V>::ld(y, i);
+        const cx<R> si = axpy(k2, VT<V>::ld(p, i), cmul(k1, yi));
+        ss.add(si, si, VT<V>::kComplex);
+        xs.add(xi, si, VT<V>::kComplex);
+        xx.add(xi, xi, VT<V>::kComplex);
+        yy.add(yi, yi, VT<V>::kComplex);
+    }
+    cdf r[4] = {ss.get_cdf(VT<V>::kComplex), xs.get_cdf(VT<V>::kComplex), xx.get_cdf(VT<V>::kComplex),
+                yy.get_cdf(VT<V>::kComplex)};
+    seg.template reduce<4>(r, kG10);
+}
+template <typename V, typename SEG>
+__global__ void __launch_bounds__(kThreads) k_upd_stu(SEG seg, const V *x, const V *y, const V *p) {
+    d_upd_stu<V, SEG>(seg, x, y, p);
+}
+
 // x <- u / |u|, y <- t / |t|; FAST also carries A x, A y by the same combinations.
 template <typename V, bool CARRY, typename SEG>
 __device__ __forceinline__ void d_upd_xy(SEG seg, V *x, V *y, const V *p, V *ax, V *ay, const V *ap) {
@@ -884,6 +916,28 @@ __global__ void k_proj_coef(State *states, int P) {
     d_proj_coef(states, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
+// |s|^2, |t|^2, |u|^2 of the update from <s,s>, <x,s>, <x,x>, <y,y> (d_upd_stu):
+// |t|^2 = |a|^2 <s,s> + b^2 <x,x> - 2 b Re(a <x,s>) with a = k0 / |s|, b = |s| (t = y when s = 0
+// under the guard), |u|^2 = |k0|^2 <x,x> + <s,s> + 2 Re(conj(k0) <x,s>)
+__device__ __forceinline__ void d_stu_coef(State *states, int P, int first, int step) {
+    FOR_ACTIVE_PROBLEMS(states, P, st) {
+        const double ss = st->red[kG10].x, xx = st->red[kG10 + 2].x, yy = st->red[kG10 + 3].x;
+        const double2 xs = st->red[kG10 + 1], k0 = st->kappa[0];
+        const double ns = sqrt(ss);
+        const double2 a = make_double2(k0.x / ns, k0.y / ns);
+        const double re_axs = a.x * xs.x - a.y * xs.y;        // Re(a <x,s>)
+        const double re_k0xs = k0.x * xs.x + k0.y * xs.y;     // Re(conj(k0) <x,s>)
+        const double tn = (st->guard && ns == 0.) ? yy : (a.x * a.x + a.y * a.y) * ss + ss * xx - 2. * ns * re_axs;
+        st->red[kSn] = make_double2(ss, 0.);
+        st->red[kTn] = make_double2(tn, 0.);
+        st->red[kUn] = make_double2((k0.x * k0.x + k0.y * k0.y) * xx + ss + 2. * re_k0xs, 0.);
+        break;
+    }
+}
+__global__ void k_stu_coef(State *states, int P) {
+    d_stu_coef(states, P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 __device__ __forceinline__ void d_refresh_mark(State *states, int P, int first, int step) {
     FOR_ACTIVE_PROBLEMS(states, P, st) {
         if (st->want_refresh) {
@@ -1046,8 +1100,13 @@ struct Phase {
         RQ_TRY(matvec(v.p, v.ap, s));
         k_gram3<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
         k_rr3<<<pgrid(), 128, 0, s>>>(states, P);
-        k_upd_s<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.y, v.p);
-        k_upd_tu<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p);
+        if (variant == RQ_LOBPCG_FAST) {
+            k_upd_stu<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p);
+            k_stu_coef<<<pgrid(), 128, 0, s>>>(states, P);
+        } else {
+            k_upd_s<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.y, v.p);
+            k_upd_tu<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p);
+        }
         if (variant == RQ_LOBPCG_REFERENCE) {
             k_upd_xy<V, false, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, v.p, nullptr, nullptr,
                                                               nullptr);
@@ -1345,8 +1404,14 @@ __global__ void __launch_bounds__(kThreads) k_persist(const PersistArgs<V> a) {
         d_gram3<V, SegPersist>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
         if (threadIdx.x == 0) d_rr3(st, 1, 0, kOnce);
         scalar_done();
-        d_upd_s<V, SegPersist>(seg, v.y, v.p);
-        d_upd_tu<V, SegPersist>(seg, v.x, v.y, v.p);
+        if (a.variant == RQ_LOBPCG_FAST) {
+            d_upd_stu<V, SegPersist>(seg, v.x, v.y, v.p);
+            if (threadIdx.x == 0) d_stu_coef(st, 1, 0, kOnce);
+            scalar_done();
+        } else {
+            d_upd_s<V, SegPersist>(seg, v.y, v.p);
+            d_upd_tu<V, SegPersist>(seg, v.x, v.y, v.p);
+        }
         if (a.variant == RQ_LOBPCG_REFERENCE) {
             d_upd_xy<V, false, SegPersist>(seg, v.x, v.y, v.p, nullptr, nullptr, nullptr);
             if (!sync()) break;
