@@ -171,7 +171,7 @@ __host__ __device__ inline size_t group_key_bytes(int J) {
 }
 
 template <typename V, int KB, bool FILTER, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : 4)
+__global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : (sizeof(V) <= 8 ? 6 : 4))
 k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int *err,
               const int *gate, const int *gate2) {
     using R = typename VT<V>::R;
