@@ -109,13 +109,17 @@ __device__ __forceinline__ bool gate_open(const int *gate, int64_t stride, const
 
 // Visit the hits of one row (warp-uniform group loop so the warp can re-converge after each
 // 64-group resolution): on_hit(g, m).  `act` rows probe; inactive lanes run the loop empty.
+// Per chunk of 64 groups the sector filter runs first and leaves a mask of the groups whose
+// target can be in the problem's sector; the bucket probes then walk only those groups, U at a
+// time per lane (random Pauli sums keep about one target in five in the sector, so most of the
+// probe work of a chunk is never issued).
 template <typename F>
 __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32_t *htab, bool act,
                                                uint64_t key, int *err, F &&on_hit) {
     const int p = act ? problem_of(key) : 0;
     const int g0 = act ? B.gofs[p] : 0;
     const int ng = act ? B.gofs[p + 1] - g0 : 0;
-    const int skip = act ? B.dgrp[p] : -1;
+    const int skip = act ? B.dgrp[p] - g0 : -1;
     const int nmax = __reduce_max_sync(0xffffffffu, ng);
     const uint64_t fa = (act && B.fmask) ? B.fmask[2 * p] : 0ULL;
     const uint64_t fbm = (act && B.fmask) ? B.fmask[2 * p + 1] : 0ULL;
@@ -126,25 +130,34 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
     const rq_subspace_t S = {nullptr, B.D, B.hkeys, B.hvals, B.hbits, RQ_LOOKUP_HASH, 64, 0,
                              B.empty_key, 0, 0, nullptr};
     const unsigned char *keys = static_cast<const unsigned char *>(B.hkeys);
+    const uint64_t *xm = B.terms.xmask + g0;
+    const uint32_t *xh = B.terms.xhash + g0;
     constexpr int U = 4;
     for (int r0 = 0; r0 < nmax; r0 += 64) {
+        const int r1 = min(ng, r0 + 64);
+        // groups of the chunk whose target passes the sector filter
+        uint64_t pass = 0ULL;
+        for (int r = r0; r < r1; ++r) {
+            const uint64_t xv = __ldg(xm + r);
+            const bool ok = r != skip && (key ^ xv) != B.empty_key &&
+                            (!B.fmask || sector_ok(fb, fa, fbm, s ^ xv));
+            pass |= (uint64_t)ok << (r - r0);
+        }
         uint64_t hot = 0ULL;
-        for (int r = r0; r < min(nmax, r0 + 64); r += U) {
+        while (__any_sync(0xffffffffu, pass != 0ULL)) {
+            int rr[U];
             uint64_t t[U];
             uint32_t b[U];
             bool q[U];
             typename KeyWidth<64>::Bucket w[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const int rr = r + u;
-                const bool in = rr < ng && rr < r0 + 64 && g0 + rr != skip;
-                const int g = g0 + (in ? rr : 0);
-                const uint64_t xv = in ? __ldg(B.terms.xmask + g) : 0ULL;
-                const uint32_t hx = in ? __ldg(B.terms.xhash + g) : 0u;
+                q[u] = pass != 0ULL;
+                rr[u] = q[u] ? __ffsll((long long)pass) - 1 : 0;
+                pass &= pass - 1ULL;
+                const uint64_t xv = q[u] ? __ldg(xm + r0 + rr[u]) : 0ULL;
+                const uint32_t hx = q[u] ? __ldg(xh + r0 + rr[u]) : 0u;
                 t[u] = key ^ xv;
-                const uint64_t ts = s ^ xv;
-                q[u] = in && (t[u] != B.empty_key) &&
-                       (!B.fmask || sector_ok(fb, fa, fbm, ts));
                 b[u] = hs ^ hx;
             }
             if (B.pbits > 0) {
@@ -165,16 +178,14 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
             for (int u = 0; u < U; ++u) {
                 bool any, open;
                 test_bucket(w[u], t[u], B.empty_key, any, open);
-                if (q[u] && (any || !open)) hot |= 1ULL << (r + u - r0);
+                if (q[u] && (any || !open)) hot |= 1ULL << rr[u];
             }
         }
         while (hot) {
-            const int rr = r0 + __ffsll((long long)hot) - 1;
+            const int r = r0 + __ffsll((long long)hot) - 1;
             hot &= hot - 1ULL;
-            const int g = g0 + rr;
-            const int m = lookup_hash_at<64>(S, key ^ __ldg(B.terms.xmask + g),
-                                             (hs ^ __ldg(B.terms.xhash + g)) >> shift, err);
-            if (m >= 0) on_hit(g, m);
+            const int m = lookup_hash_at<64>(S, key ^ __ldg(xm + r), (hs ^ __ldg(xh + r)) >> shift, err);
+            if (m >= 0) on_hit(g0 + r, m);
         }
         __syncwarp();
     }
@@ -182,7 +193,7 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
 
 // FREE-mode batched matvec: thread per row.
 template <typename V>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
 k_batch_matvec_free(const rq_batch_t B, const V *__restrict__ x, V *__restrict__ y, int *err,
                     const int *gate, int64_t gstride, const int *gate2) {
     using R = typename VT<V>::R;
