@@ -161,7 +161,9 @@ __device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, ui
 // is not interleaved with the probes.
 
 // Group keys live in shared memory for the whole launch: (x_j, h(x_j)) packed as uint2 for 32-bit
-// keys (8 B per group) or as uint64 + uint32 arrays for 64-bit keys (12 B per group).  Large J
+// keys (8 B per group) or as uint64 + uint32 arrays for 64-bit keys (12 B per group).  The x = 0
+// group is left out of the list (its diagonal is applied before the probes), so that the probe
+// loop has no per-group skip test; resident index c is group c + (c >= diag_group).  Large J
 // runs one 1024-thread block per SM so that up to kMaxResidentGroups fit.
 constexpr int kMaxResidentGroups = 16384;
 
@@ -170,70 +172,75 @@ __host__ __device__ inline size_t group_key_bytes(int J) {
     return KB == 32 ? (size_t)J * 8 : align16((size_t)J * 8) + (size_t)J * 4;
 }
 
-template <typename V, int KB, bool FILTER, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : (sizeof(V) <= 8 ? 6 : 4))
-k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int *err,
-              const int *gate, const int *gate2) {
+// Sector filter of the hash kernel: none, the general (popcount a, popcount b) bitset, or the
+// common case of a subspace in one sector (a single bit set: two popcount compares, no table).
+enum { kFiltNone = 0, kFiltSet = 1, kFiltPoint = 2 };
+
+// shared memory of the hash kernel: the sector bitset, the hash byte tables (64-bit keys use
+// all eight) and, in dynamic shared memory, the resident group keys
+__shared__ uint32_t hk_fb[RQ_FILTER_WORDS];
+__shared__ uint32_t hk_htab[kHashTableWords];
+extern __shared__ __align__(16) unsigned char hk_dyn[];
+
+template <typename V, int KB, int FM>
+__device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__restrict__ x,
+                                          V *__restrict__ y, int *err, int pa0, int pb0) {
     using R = typename VT<V>::R;
     using K = typename KeyWidth<KB>::K;
     constexpr int NB = KeyWidth<KB>::kNbytes;
     constexpr int kBucketBytes = KeyWidth<KB>::kBucketBytes;
-    constexpr int U = (KB == 32) ? 8 : 4;  // probes in flight per thread
-    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ uint32_t fb[RQ_FILTER_WORDS];
-    __shared__ uint32_t htab[NB * 256];
+    constexpr int U = (KB == 32) ? 4 : 4;
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
-    const int J = T.J;
-    // group keys: gk32[j] = (x_j, h_j) for 32-bit keys; gx64[j], gh64[j] for 64-bit keys
-    uint2 *gk32 = reinterpret_cast<uint2 *>(smem);
-    uint64_t *gx64 = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *gh64 = reinterpret_cast<uint32_t *>(smem + align16((size_t)J * 8));
-    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) fb[w] = S.fbits[w];
-    init_hash_tables(htab, NB);
-    __syncthreads();
-    for (int j = threadIdx.x; j < J; j += blockDim.x) {
-        const uint64_t xv = T.xmask[j];
-        const uint32_t h = T.xhash ? T.xhash[j] : lin_hash(htab, xv, NB);
-        if (KB == 32) {
-            gk32[j] = make_uint2((uint32_t)xv, h);
-        } else {
-            gx64[j] = xv;
-            gh64[j] = h;
-        }
-    }
-    __syncthreads();
-
     const int64_t D = S.D;
     const int skip = T.diag_group;  // the x = 0 group is applied outside the probe loop
+    const int nres = T.J - (skip >= 0 ? 1 : 0);  // resident groups
+    const uint2 *gk32 = reinterpret_cast<const uint2 *>(hk_dyn);
+    const uint64_t *gx64 = reinterpret_cast<const uint64_t *>(hk_dyn);
+    const uint32_t *gh64 = reinterpret_cast<const uint32_t *>(hk_dyn + align16((size_t)T.J * 8));
     const bool d0 = (op.diag0 != nullptr) && (skip >= 0);
     const K fa = (K)S.fmask_a, fbm = (K)S.fmask_b, empty = (K)S.empty_key;
     const int shift = 32 - S.hbits;
     const uint32_t *pmap = S.pbits > 0 ? S.pmap : nullptr;
     const int pshift = 32 - S.pbits;
     const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
-    // Every lane runs the same row batches and super-chunks (lanes past D with nothing to do),
-    // so that the warp can be re-converged after each super-chunk's hot-group resolution; without
-    // the explicit __syncwarp the lanes that took the rare path stay split from the rest for the
-    // remainder of the row.
+    auto sector = [&](K t) -> bool {
+        if (FM == kFiltPoint) {
+            int pa, pb;
+            if (sizeof(K) == 8) {
+                pa = __popcll((unsigned long long)(t & fa));
+                pb = __popcll((unsigned long long)(t & fbm));
+            } else {
+                pa = __popc((unsigned)(t & fa));
+                pb = __popc((unsigned)(t & fbm));
+            }
+            return (pa == pa0) & (pb == pb0);
+        }
+        if (FM == kFiltSet) return sector_ok_k<K>(hk_fb, fa, fbm, t);
+        return true;
+    };
+    // Every lane runs the same row batches and super-chunks, so that the warp can be
+    // re-converged after each super-chunk's hot-group resolution; without the explicit
+    // __syncwarp the lanes that took the rare path stay split from the rest for the remainder of
+    // the row.  Lanes past D probe the last row again and store nothing.
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < D;
          base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = base + threadIdx.x;
         const bool active = i < D;
-        const uint64_t s64 = active ? __ldg(S.states + i) : 0ULL;
+        const int64_t ir = active ? i : D - 1;
+        const uint64_t s64 = __ldg(S.states + ir);
         const K s = (K)s64;
-        const uint32_t hs = lin_hash(htab, s64, NB);
+        const uint32_t hs = lin_hash(hk_htab, s64, NB);
         CAcc<R> acc;
-        const cx<R> xi = active ? VT<V>::ld(x, i) : cx<R>{(R)0, (R)0};
-        if (active && d0) {
-            const R dv = (R)op.diag0[i];
+        const cx<R> xi = VT<V>::ld(x, ir);
+        if (d0) {
+            const R dv = (R)op.diag0[ir];
             acc.add({dv * xi.re, dv * xi.im});
-        } else if (active && skip >= 0) {
+        } else if (skip >= 0) {
             acc.add(cmul(group_diag<R>(T, skip, s64), xi));
         }
-        for (int gs0 = 0; gs0 < J; gs0 += 64) {
-            const int gs1 = min(J, gs0 + 64);
+        for (int gs0 = 0; gs0 < nres; gs0 += 64) {
+            const int gs1 = min(nres, gs0 + 64);
             uint64_t hot = 0ULL;
             int g = gs0;
             for (; g + U <= gs1; g += U) {
@@ -252,11 +259,9 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
                         t[u] = s ^ (K)gx64[g + u];
                         hxg = gh64[g + u];
                     }
-                    q[u] = active && (g + u != skip);
-                    if (FILTER) q[u] = q[u] && sector_ok_k<K>(fb, fa, fbm, t[u]);
+                    q[u] = sector(t[u]);
                     b[u] = hs ^ hxg;
                 }
-
                 if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
                     uint32_t pw[U];
 #pragma unroll
@@ -271,24 +276,25 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
                 for (int u = 0; u < U; ++u)
                     w[u] = KeyWidth<KB>::load(keys + (size_t)(b[u] >> shift) * kBucketBytes, q[u],
                                               S.empty_key);
+                uint32_t hb = 0u;  // hot bits of this batch, constant shifts
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     bool any, open;
                     test_bucket(w[u], t[u], empty, any, open);
-                    hot |= (uint64_t)(q[u] && (any || !open)) << (g + u - gs0);
+                    if (q[u] && (any || !open)) hb |= 1u << u;
                 }
+                hot |= (uint64_t)hb << (g - gs0);
             }
             for (; g < gs1; ++g) {  // tail: mark and resolve below
                 const K t = s ^ (KB == 32 ? (K)gk32[g].x : (K)gx64[g]);
-                bool ok = active && (g != skip);
-                if (FILTER) ok = ok && sector_ok_k<K>(fb, fa, fbm, t);
-                if (ok) hot |= 1ULL << (g - gs0);
+                if (sector(t)) hot |= 1ULL << (g - gs0);
             }
             while (hot) {
-                const int gg = gs0 + __ffsll((long long)hot) - 1;
+                const int gc = gs0 + __ffsll((long long)hot) - 1;
                 hot &= hot - 1ULL;
+                const int gg = gc + (skip >= 0 && gc >= skip);
                 const uint64_t xv = __ldg(T.xmask + gg);
-                const uint32_t hxg = KB == 32 ? gk32[gg].y : gh64[gg];
+                const uint32_t hxg = KB == 32 ? gk32[gc].y : gh64[gc];
                 const int m = lookup_hash_at<KB>(S, s64 ^ xv, (hs ^ hxg) >> shift, err);
                 if (m >= 0) acc.add(cmul(group_diag<R>(T, gg, s64), VT<V>::ld(x, m)));
             }
@@ -296,6 +302,54 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
         }
         if (active) VT<V>::st(y, i, acc.get());
     }
+}
+
+template <typename V, int KB, bool FILTER, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : (sizeof(V) <= 8 ? 6 : 4))
+k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int *err,
+              const int *gate, const int *gate2) {
+    constexpr int NB = KeyWidth<KB>::kNbytes;
+    if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
+    __shared__ int s_fcount, s_fbit;
+    unsigned char *smem = hk_dyn;
+    const rq_subspace_t &S = op.sub;
+    const rq_terms_t &T = op.terms;
+    const int J = T.J;
+    const int skip = T.diag_group;
+    uint32_t *htab = hk_htab;
+    if (threadIdx.x == 0) {
+        s_fcount = 0;
+        s_fbit = 0;
+    }
+    init_hash_tables(htab, NB);
+    __syncthreads();
+    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) {
+        const uint32_t v = S.fbits[w];
+        hk_fb[w] = v;
+        if (FILTER && v) {
+            atomicAdd(&s_fcount, __popc(v));
+            atomicMax(&s_fbit, w * 32 + 31 - __clz(v));
+        }
+    }
+    for (int j = threadIdx.x; j < J; j += blockDim.x) {
+        if (j == skip) continue;
+        const int r = j - (skip >= 0 && j > skip);
+        const uint64_t xv = T.xmask[j];
+        const uint32_t h = T.xhash ? T.xhash[j] : lin_hash(htab, xv, NB);
+        if (KB == 32) {
+            reinterpret_cast<uint2 *>(smem)[r] = make_uint2((uint32_t)xv, h);
+        } else {
+            reinterpret_cast<uint64_t *>(smem)[r] = xv;
+            reinterpret_cast<uint32_t *>(smem + align16((size_t)J * 8))[r] = h;
+        }
+    }
+    __syncthreads();
+    if (!FILTER)
+        hash_rows<V, KB, kFiltNone>(op, x, y, err, 0, 0);
+    else if (s_fcount == 1)
+        hash_rows<V, KB, kFiltPoint>(op, x, y, err, s_fbit / 65, s_fbit % 65);
+    else
+        hash_rows<V, KB, kFiltSet>(op, x, y, err, 0, 0);
 }
 
 // xhash[j] = h(xmask[j])

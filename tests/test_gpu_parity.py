@@ -311,3 +311,40 @@ def test_persistent_loop_matches_graph_loop(cache_level, variant):
         assert abs(i1['niter'] - i2['niter']) <= 1, (i1, i2)
         assert i1['converged'] and i2['converged']
         assert abs(torch.vdot(x1, x2).item()) > 1 - 1e-10
+
+
+@pytest.mark.parametrize('key_bits', [32, 64])
+@pytest.mark.parametrize('sectors', ['one', 'two', 'off'])
+def test_hash_kernel_sector_filter_modes(sectors, key_bits):
+    """The FREE hash kernel's three filter forms -- a subspace in one (popcount a, popcount b)
+    sector (two popcount compares), several sectors (the bitset) and the filter off -- give the
+    oracle's product, and all three agree bit for bit with each other."""
+    import torch
+    from oracle import sqd as osqd
+    from oracle.paulis import from_paulisum as oterms
+    from rqutils_gb300 import workloads
+    from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    rng = np.random.default_rng(404)
+    n = 16
+    labels, coeffs = workloads.random_pauli_sum(rng, n, 300)
+    S1 = workloads.sample_sector(rng, 3000, [(8, 4), (8, 4)])
+    if sectors == 'two':
+        S = np.union1d(S1, workloads.sample_sector(rng, 1500, [(8, 3), (8, 5)]))
+    else:
+        S = S1
+    h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
+    ot = oterms((labels, coeffs), force_real=True)
+    v = workloads.random_vector(rng, len(S))
+    ref = osqd.matvec_xcached(v, osqd.xsources_all(S, ot), ot, S)
+    fm = (0, 0) if sectors == 'off' else None
+    sub = DeviceSubspace(S, num_qubits=n, filter_masks=fm, key_bits=key_bits)
+    bits = int(np.bitwise_count(sub.fbits.cpu().numpy().view(np.uint32)).sum())
+    assert bits == {'one': 1, 'two': 2, 'off': bits}[sectors]
+    op = DeviceOperator(DeviceTerms(h), sub, mode='free')
+    y = op.matvec(torch.as_tensor(v).cuda()).cpu().numpy()
+    op.check_errors()
+    assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref)
+    other = DeviceSubspace(S, num_qubits=n, filter_masks=(0, 0), key_bits=key_bits)
+    y0 = DeviceOperator(DeviceTerms(h), other, mode='free').matvec(torch.as_tensor(v).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(y, y0)
