@@ -189,7 +189,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
     using K = typename KeyWidth<KB>::K;
     constexpr int NB = KeyWidth<KB>::kNbytes;
     constexpr int kBucketBytes = KeyWidth<KB>::kBucketBytes;
-    constexpr int U = (KB == 32) ? 4 : 4;
+    constexpr int U = 4;  // probes in flight per thread (no spills at 40 registers)
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
     const int64_t D = S.D;
