@@ -357,6 +357,67 @@ __device__ __forceinline__ void block_sum(cdf (&w)[NV], cdf (*red)[NV]) {
     }
 }
 
+// Block-wide sums of NV <= 8 values, left in tot[0..NV) (shared memory) for every thread.
+// Within a warp the values are reduce-scattered: at each of the first log2(P) butterfly steps
+// (P = NV rounded up to a power of two) a lane keeps half of its values and receives the
+// partner's partial sums of that half, so a lane adds P - 1 + (5 - log2 P) pairs instead of
+// 5 NV; afterwards the lanes of one value hold its warp total.  Across warps, warp k sums
+// value k.  The order of every addition is fixed, so each block computes the same sums from
+// the same inputs.
+template <int NV>
+__device__ __forceinline__ void block_sum_all(cdf (&w)[NV], cdf *tot, cdf (*red)[NV]) {
+    static_assert(NV >= 1 && NV <= 8, "block_sum_all: at most 8 values");
+    constexpr int L = NV <= 1 ? 0 : NV <= 2 ? 1 : NV <= 4 ? 2 : 3;  // halving steps
+    constexpr int P = 1 << L;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarp = (blockDim.x + 31) >> 5;
+    cdf a[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) a[k] = k < NV ? w[k] : cdf_zero();
+#pragma unroll
+    for (int s = 0; s < L; ++s) {
+        const int o = 16 >> s, h = P >> (s + 1);
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+            const cdf mine = up ? a[h + j] : a[j];
+            const cdf other = up ? a[j] : a[h + j];
+            a[j] = cdf_add(mine, cdf_shfl_xor(other, o));
+        }
+    }
+#pragma unroll
+    for (int s = L; s < 5; ++s) a[0] = cdf_add(a[0], cdf_shfl_xor(a[0], 16 >> s));
+    int v = 0;
+#pragma unroll
+    for (int s = 0; s < L; ++s) v += ((lane >> (4 - s)) & 1) * (P >> (s + 1));
+    if ((lane & ((32 >> L) - 1)) == 0 && v < NV) red[warp][v] = a[0];
+    __syncthreads();
+    for (int k = warp; k < NV; k += nwarp) {
+        cdf t = lane < nwarp ? red[lane][k] : cdf_zero();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = cdf_add(t, cdf_shfl_xor(t, o));
+        if (lane == 0) tot[k] = t;
+    }
+    __syncthreads();
+}
+
+// Sums of NV values over n per-block partials (float4-packed double-floats, stride `stride`),
+// warp k summing value k; left in tot[0..NV) for every thread.
+template <int NV>
+__device__ __forceinline__ void partials_sum(const float4 *part, int n, int stride, cdf *tot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarp = (blockDim.x + 31) >> 5;
+    for (int k = warp; k < NV; k += nwarp) {
+        cdf t = cdf_zero();
+#pragma unroll 4
+        for (int b = lane; b < n; b += 32) t = cdf_add(t, cdf_unpack(__ldcg(part + (size_t)b * stride + k)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = cdf_add(t, cdf_shfl_xor(t, o));
+        if (lane == 0) tot[k] = t;
+    }
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------------------------------
 // deterministic grid reduction of NV complex values
 // ------------------------------------------------------------------------------------------
@@ -366,40 +427,30 @@ __device__ __forceinline__ void block_sum(cdf (&w)[NV], cdf (*red)[NV]) {
 template <int NV>
 __device__ void grid_reduce(cdf (&v)[NV], void *scratch, double2 *out) {
     __shared__ cdf red[kThreads / 32][NV];
+    __shared__ cdf tot[NV];
     __shared__ bool last;
     unsigned int *counter = reinterpret_cast<unsigned int *>(scratch);
     float4 *part = reinterpret_cast<float4 *>(reinterpret_cast<char *>(scratch) + 16);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     cdf w[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) w[k] = v[k];
-    block_sum<NV>(w, red);
-    if (warp == 0) {
-        if (lane == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) part[(size_t)blockIdx.x * NV + k] = cdf_pack(w[k]);
-            __threadfence();
-            const unsigned int t = atomicAdd(counter, 1u);
-            last = (t == gridDim.x - 1);
-        }
+    block_sum_all<NV>(w, tot, red);
+    if (threadIdx.x < NV) {
+        part[(size_t)blockIdx.x * NV + threadIdx.x] = cdf_pack(tot[threadIdx.x]);
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        cdf a = cdf_zero();
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-            a = cdf_add(a, cdf_unpack(__ldcg(part + (size_t)b * NV + k)));
-        w[k] = a;
-    }
-    __syncthreads();  // red[] reuse
-    block_sum<NV>(w, red);
-    if (warp == 0 && lane == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) out[k] = cdf_val(w[k]);
-        *counter = 0u;
-    }
+    partials_sum<NV>(part, (int)gridDim.x, NV, tot);
+    if (threadIdx.x < NV) out[threadIdx.x] = cdf_val(tot[threadIdx.x]);
+    if (threadIdx.x == 0) *counter = 0u;
 }
 
 // Max blocks a reducing launch may use (sizes the partials of the scratch area).

@@ -1288,34 +1288,24 @@ struct SegPersist {
     template <int NV>
     __device__ void reduce(cdf (&v)[NV], int slot) const {
         __shared__ cdf red[kThreads / 32][NV];
+        __shared__ cdf tot[NV];
         cdf w[NV];
         float4 *pb = part + (size_t)(*flip) * gridDim.x * kMaxReduce;
 #pragma unroll
         for (int k = 0; k < NV; ++k) w[k] = v[k];
-        block_sum<NV>(w, red);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) pb[(size_t)blockIdx.x * kMaxReduce + k] = cdf_pack(w[k]);
+        block_sum_all<NV>(w, tot, red);
+        if (threadIdx.x < NV) {
+            pb[(size_t)blockIdx.x * kMaxReduce + threadIdx.x] = cdf_pack(tot[threadIdx.x]);
+            __threadfence();
         }
         if (!grid_sync(bar, passed)) {
             if (threadIdx.x == 0) st->active = 0;  // aborted: every block stops
             __syncthreads();
             return;
         }
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            cdf acc = cdf_zero();
-            for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-                acc = cdf_add(acc, cdf_unpack(__ldcg(pb + (size_t)b * kMaxReduce + k)));
-            w[k] = acc;
-        }
-        __syncthreads();  // red[] reuse
-        block_sum<NV>(w, red);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) st->red[slot + k] = cdf_val(w[k]);
-            *flip ^= 1;
-        }
+        partials_sum<NV>(pb, (int)gridDim.x, kMaxReduce, tot);
+        if (threadIdx.x < NV) st->red[slot + threadIdx.x] = cdf_val(tot[threadIdx.x]);
+        if (threadIdx.x == 0) *flip ^= 1;
         __syncthreads();
     }
 };

@@ -223,7 +223,7 @@ def hubbard_family(S, Us, Lx=4, Ly=4, t=1.0, periodic=True, target_rel=1e-7, max
 
 
 def evaluate_starts(model, S, Us, Lx=4, Ly=4, t=1.0, periodic=True, target_rel=1e-8,
-                    maxiter=5000, seed=0, device=None, mixed=True, variant='fast'):
+                    maxiter=5000, seed=0, device=None, mixed=True, variant='fast', jacobi=False):
     """LOBPCG to |r| <= target_rel |theta| on each U from three start vectors: the network's
     ('learned', inference included in the time), a seeded random vector ('random') and the
     reference's one-hot at the lowest diagonal entry ('reference').  Returns {start: [dict]}."""
@@ -248,7 +248,7 @@ def evaluate_starts(model, S, Us, Lx=4, Ly=4, t=1.0, periodic=True, target_rel=1
                 x0 = torch.zeros(sub.D, dtype=torch.float64, device=dev)
                 x0[int(torch.argmin(op.diag0))] = 1.
             e, x, info = lobpcg_solve(op, x0, maxiter=maxiter, target_rel=target_rel,
-                                      variant=variant, mixed=mixed)
+                                      variant=variant, mixed=mixed, jacobi=jacobi)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
             ax = op.matvec(x)
