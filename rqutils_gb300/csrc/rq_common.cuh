@@ -334,29 +334,6 @@ __device__ __forceinline__ cdf cdf_zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
 __device__ __forceinline__ float4 cdf_pack(cdf a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
 __device__ __forceinline__ cdf cdf_unpack(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
 
-// Block-wide sum of NV values (every thread passes its own); the result is valid in warp 0,
-// lane 0.  `red` is shared scratch of [warps][NV].
-template <int NV>
-__device__ __forceinline__ void block_sum(cdf (&w)[NV], cdf (*red)[NV]) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nwarp = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) w[k] = cdf_add(w[k], cdf_shfl_xor(w[k], o));
-        if (lane == 0) red[warp][k] = w[k];
-    }
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            w[k] = (lane < nwarp) ? red[lane][k] : cdf_zero();
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) w[k] = cdf_add(w[k], cdf_shfl_xor(w[k], o));
-        }
-    }
-}
-
 // Block-wide sums of NV <= 8 values, left in tot[0..NV) (shared memory) for every thread.
 // Within a warp the values are reduce-scattered: at each of the first log2(P) butterfly steps
 // (P = NV rounded up to a power of two) a lane keeps half of its values and receives the

@@ -180,17 +180,20 @@ struct SegBatch {
     template <int NV>
     __device__ void reduce(cdf (&v)[NV], int slot) const {
         __shared__ cdf red[kThreads / 32][NV];
+        __shared__ cdf tot[NV];
         __shared__ bool last;
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const int c = blockIdx.x, p = cprob[c];
         float4 *pt = reinterpret_cast<float4 *>(part);
         cdf w[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) w[k] = v[k];
-        block_sum<NV>(w, red);
-        if (warp == 0 && lane == 0) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) pt[(size_t)c * kMaxReduce + k] = cdf_pack(w[k]);
+        block_sum_all<NV>(w, tot, red);
+        if (threadIdx.x < NV) {
+            pt[(size_t)c * kMaxReduce + threadIdx.x] = cdf_pack(tot[threadIdx.x]);
+            __threadfence();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
             __threadfence();
             const unsigned int n = (unsigned int)(cofs[p + 1] - cofs[p]);
             last = (atomicAdd(counter + p, 1u) == n - 1);
@@ -748,13 +751,16 @@ __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2
     c0 -= 2. * (t.x * m21.x - t.y * m21.y);
     const double p = c2 * c2 - 3. * c1;
     const double q = -13.5 * c0 - c2 * c2 * c2 + 4.5 * c2 * c1;
-    const double phi = atan2(sqrt(27. * (0.25 * c1 * c1 * (p - c1) + c0 * (q + 6.75 * c0))), q) / 3.;
+    // divisions by 3 as products with 1/3 (GB300 runs an FP64 division as a long FP64 sequence
+    // on one thread here; the results differ from the quotients by at most an ulp)
+    constexpr double kThird = 1. / 3.;
+    const double phi = atan2(sqrt(27. * (0.25 * c1 * c1 * (p - c1) + c0 * (q + 6.75 * c0))), q) * kThird;
     const double cp = cos(phi), sp = sin(phi), s3 = sqrt(3.);
     double xmin = 2. * cp;
     xmin = fmin(xmin, -cp - s3 * sp);
     xmin = fmin(xmin, -cp + s3 * sp);
     if (isnan(cp) || isnan(sp)) xmin = NAN;  // jnp.min propagates NaN
-    lam = sqrt(p) / 3. * xmin - c2 / 3.;
+    lam = sqrt(p) * kThird * xmin - c2 * kThird;
     // columns 1 and 2 of (A - lambda I): a = (m01, m11 - l, m21), b = (m02, m12, m22 - l)
     const double2 a0 = make_double2(m10.x, -m10.y), a1 = make_double2(m11.x - lam, m11.y), a2 = m21;
     const double2 b0 = m02, b1 = make_double2(m21.x, -m21.y), b2 = make_double2(m22.x - lam, m22.y);
@@ -799,7 +805,8 @@ __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2
             nrm = 1.;
         }
     }
-    for (int k = 0; k < 3; ++k) v[k] = make_double2(c[k].x / nrm, c[k].y / nrm);
+    const double inv = 1. / nrm;
+    for (int k = 0; k < 3; ++k) v[k] = make_double2(c[k].x * inv, c[k].y * inv);
 }
 
 __device__ __forceinline__ void d_rr3(State *states, int P, int first, int step) {
