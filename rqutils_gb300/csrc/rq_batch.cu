@@ -135,13 +135,27 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
     constexpr int U = 4;
     for (int r0 = 0; r0 < nmax; r0 += 64) {
         const int r1 = min(ng, r0 + 64);
-        // groups of the chunk whose target passes the sector filter
+        // groups of the chunk whose target passes the sector filter, four at a time so that
+        // their X-mask and filter-word loads overlap
         uint64_t pass = 0ULL;
-        for (int r = r0; r < r1; ++r) {
-            const uint64_t xv = __ldg(xm + r);
-            const bool ok = r != skip && (key ^ xv) != B.empty_key &&
-                            (!B.fmask || sector_ok(fb, fa, fbm, s ^ xv));
-            pass |= (uint64_t)ok << (r - r0);
+        for (int r = r0; r < r1; r += 4) {
+            uint64_t xv[4];
+            int bit[4];
+            uint32_t fw[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xv[u] = r + u < r1 ? __ldg(xm + r + u) : 0ULL;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint64_t ts = s ^ xv[u];
+                bit[u] = __popcll(ts & fa) * 65 + __popcll(ts & fbm);
+                fw[u] = (r + u < r1 && B.fmask) ? __ldg(fb + (bit[u] >> 5)) : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool ok = r + u < r1 && r + u != skip && (key ^ xv[u]) != B.empty_key &&
+                                ((fw[u] >> (bit[u] & 31)) & 1u);
+                if (ok) pass |= 1ULL << (r + u - r0);
+            }
         }
         uint64_t hot = 0ULL;
         while (__any_sync(0xffffffffu, pass != 0ULL)) {
