@@ -365,28 +365,39 @@ k_mask(SEG seg, const V *v, V *p) {
     d_mask<V, SEG>(seg, v, p);
 }
 
-// FAST projection, last step: p = v / |v|, or 0 when |v| < thr |r| (r numerically inside the span
-// of x, y; the role of the 0.99 cut of ground_locg.py:421); |v|^2 in red[kVn], |r|^2 in red[kG10 + 5]
+// FAST projection in one pass, no reduction: p = m (v - d0 x - d1 y) with d0, d1 from
+// red[kIp0], red[kIp1] and w = |v - d0 x - d1 y|^2 in red[kVn] (all three from the six inner
+// products, d_proj_coef); m = 1 / sqrt(w), or 0 when w < thr^2 |v|^2 (v numerically inside the
+// span of x, y; the role of the 0.99 cut of ground_locg.py:421), |v|^2 in red[kG10 + 5].
 template <typename V, typename SEG>
-__device__ __forceinline__ void d_norm_mask(SEG seg, const V *v, V *p) {
+__device__ __forceinline__ void d_sub2_scale(SEG seg, const V *x, const V *y, const V *v, V *p) {
     State *st = seg.state();
     GATE(st);
     using R = typename VT<V>::R;
-    BLOCK_R(1, {
+    BLOCK_R(5, {
         const double n2 = st->red[kVn].x;
         const double r2 = st->red[kG10 + 5].x;
         const double thr = sizeof(R) == 4 ? 1e-5 : 1e-10;
-        out[0] = (R)((n2 > 0. && n2 > thr * thr * r2) ? 1. / sqrt(n2) : 0.);
+        const double m = (n2 > 0. && n2 > thr * thr * r2) ? 1. / sqrt(n2) : 0.;
+        out[0] = (R)m;
+        out[1] = (R)(-m * st->red[kIp0].x);
+        out[2] = (R)(-m * st->red[kIp0].y);
+        out[3] = (R)(-m * st->red[kIp1].x);
+        out[4] = (R)(-m * st->red[kIp1].y);
     })
     const R m = br_[0];
+    const cx<R> a0 = {br_[1], br_[2]}, a1 = {br_[3], br_[4]};
     SEG_LOOP(i) {
-        cx<R> w = VT<V>::ld(v, i);
-        VT<V>::st(p, i, {w.re * m, w.im * m});
+        const cx<R> vi = VT<V>::ld(v, i);
+        cx<R> w = axpy(a0, VT<V>::ld(x, i), {vi.re * m, vi.im * m});
+        w = axpy(a1, VT<V>::ld(y, i), w);
+        VT<V>::st(p, i, w);
     }
 }
 template <typename V, typename SEG>
-__global__ void __launch_bounds__(kThreads) k_norm_mask(SEG seg, const V *v, V *p) {
-    d_norm_mask<V, SEG>(seg, v, p);
+__global__ void __launch_bounds__(kThreads)
+k_sub2_scale(SEG seg, const V *x, const V *y, const V *v, V *p) {
+    d_sub2_scale<V, SEG>(seg, x, y, v, p);
 }
 
 // Gram entries of (x, y, p): <y,Ax> <p,Ax> <p,Ay> <x,Ax> <y,Ay> <p,Ap>
@@ -914,8 +925,18 @@ __device__ __forceinline__ void d_proj_coef(State *states, int P, int first, int
         const double2 gyx = make_double2(gxy.x, -gxy.y);  // <y, x>
         const double2 ax = mul(gxx, cx_), bx = mul(gxy, cy);
         const double2 ay = mul(gyx, cx_), by = mul(gyy, cy);
-        st->red[kIp0] = make_double2(2. * cx_.x - ax.x - bx.x, 2. * cx_.y - ax.y - bx.y);
-        st->red[kIp1] = make_double2(2. * cy.x - ay.x - by.x, 2. * cy.y - ay.y - by.y);
+        const double2 d0 = make_double2(2. * cx_.x - ax.x - bx.x, 2. * cx_.y - ax.y - bx.y);
+        const double2 d1 = make_double2(2. * cy.x - ay.x - by.x, 2. * cy.y - ay.y - by.y);
+        st->red[kIp0] = d0;
+        st->red[kIp1] = d1;
+        // |r - d0 x - d1 y|^2 = <r,r> - 2 Re(conj(d0) <x,r> + conj(d1) <y,r>) + |d0|^2 <x,x>
+        //                       + |d1|^2 <y,y> + 2 Re(conj(d0) d1 <x,y>)
+        const double2 d0c = make_double2(d0.x, -d0.y), d1c = make_double2(d1.x, -d1.y);
+        const double2 d01 = mul(d0c, d1);
+        const double n2 = st->red[kG10 + 5].x - 2. * (mul(d0c, cx_).x + mul(d1c, cy).x) +
+                          (d0.x * d0.x + d0.y * d0.y) * gxx.x + (d1.x * d1.x + d1.y * d1.y) * gyy.x +
+                          2. * mul(d01, gxy).x;
+        st->red[kVn] = make_double2(n2, 0.);
         break;
     }
 }
@@ -1076,8 +1097,7 @@ struct Phase {
             Pairs<V, 6> g{{v.x, v.y, v.x, v.x, v.y, src}, {src, src, v.x, v.y, v.y, src}};
             k_dots<V, 6, SEG><<<grid, kThreads, 0, s>>>(seg, g, kG10);
             k_proj_coef<<<pgrid(), 128, 0, s>>>(states, P);
-            k_sub2_norm<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src);
-            k_norm_mask<V, SEG><<<grid, kThreads, 0, s>>>(seg, src, v.p);
+            k_sub2_scale<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.x, v.y, src, v.p);
             return;
         }
         Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
@@ -1378,8 +1398,7 @@ __global__ void __launch_bounds__(kThreads) k_persist(const PersistArgs<V> a) {
             d_dots<V, 6, SegPersist>(seg, g, kG10);
             if (threadIdx.x == 0) d_proj_coef(st, 1, 0, kOnce);
             scalar_done();
-            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-            d_norm_mask<V, SegPersist>(seg, src, v.p);
+            d_sub2_scale<V, SegPersist>(seg, v.x, v.y, src, v.p);
         } else {
             Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
             d_dots<V, 2, SegPersist>(seg, pr, kIp0);
