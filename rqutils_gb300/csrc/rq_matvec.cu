@@ -154,11 +154,12 @@ __device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, ui
 // ------------------------------------------------------------------------------------------
 // One thread per row.  Per row: h(s) once; per X group: t = s ^ x_j, sector filter,
 // bucket = (h(s) ^ h(x_j)) >> shift, one bucket load.  The per-group data (x_j, h(x_j)) is read
-// with warp-uniform loads that stay in L1, so any number of groups streams without staging;
-// the terms of a group are read from global memory only on a hit.  U bucket loads are issued
-// together; the loop only marks "hot" groups (a key match, a full bucket, or a target equal to
-// the empty key) in a 64-bit mask, resolved once per 64 groups so that the rare divergent work
-// is not interleaved with the probes.
+// with broadcast shared-memory loads (every thread walks the same group sequence); the terms of
+// a group are read from global memory only on a hit.  U bucket loads are issued together; the
+// loop only marks "hot" groups (a key match, a full bucket, or a target equal to the empty key)
+// in a 64-bit mask, resolved once per 64 groups so that the rare divergent work is not
+// interleaved with the probes.  The limit at D = 2^20 (tables in L2) is the L1 data pipe: each
+// bucket load is one 16- or 32-byte read at a random address, one wavefront per lane.
 
 // Group keys live in shared memory for the whole launch: (x_j, h(x_j)) packed as uint2 for 32-bit
 // keys (8 B per group) or as uint64 + uint32 arrays for 64-bit keys (12 B per group).  The x = 0
