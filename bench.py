@@ -162,14 +162,19 @@ class ClockSampler:
 # ---------------------------------------------------------------------------------------------
 # distributed helpers (replicas only: every rank runs the same single-GPU workload)
 # ---------------------------------------------------------------------------------------------
-def dist_init():
+def dist_init(backend=None):
+    """Replica ranks from the torchrun environment: NCCL with one GPU per rank (LOCAL_RANK) when
+    CUDA is present, else gloo (host-side checks of the replica logic)."""
     import torch
     ws = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     if ws > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
-        dist.init_process_group('nccl')
+        if backend is None:
+            backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        if backend == 'nccl':
+            torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+        dist.init_process_group(backend)
     return rank, ws
 
 
@@ -184,9 +189,16 @@ def max_over_ranks(v, ws):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device='cuda')
+    dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(units, seconds, ws):
+    """Whole-job rate of ws independent replicas: each rank processed `units` in its own
+    `seconds`; the job took as long as its slowest rank."""
+    return ws * units / max_over_ranks(seconds, ws)
 
 
 # ---------------------------------------------------------------------------------------------
