@@ -324,7 +324,6 @@ __device__ __forceinline__ df df_add(df a, df b) {
     return {s, e};
 }
 __device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
-__device__ __forceinline__ cdf cdf_of(double2 v) { return {df_of(v.x), df_of(v.y)}; }
 __device__ __forceinline__ double2 cdf_val(cdf a) { return make_double2(df_val(a.re), df_val(a.im)); }
 __device__ __forceinline__ cdf cdf_shfl_xor(cdf a, int o) {
     return {{__shfl_xor_sync(0xffffffffu, a.re.hi, o), __shfl_xor_sync(0xffffffffu, a.re.lo, o)},

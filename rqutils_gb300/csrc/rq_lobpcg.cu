@@ -118,9 +118,6 @@ struct CDot {
 };
 
 template <typename R>
-__device__ __forceinline__ cx<R> c_of(double2 v) { return {(R)v.x, (R)v.y}; }
-
-template <typename R>
 __device__ __forceinline__ cx<R> axpy(cx<R> a, cx<R> x, cx<R> y) {  // a*x + y
     return {a.re * x.re - a.im * x.im + y.re, a.re * x.im + a.im * x.re + y.im};
 }
