@@ -85,6 +85,18 @@ typedef struct rq_subspace {
     uint32_t *pmap;          /* [2^pbits / 32]: bit (hash(s) >> (32 - pbits)) set for every
                                 state, written by rq_subspace_build; a lookup whose bit is
                                 clear skips the table (NULL = none)                        */
+    uint32_t *htags;         /* [1 << hbits] (4 bytes per bucket) or NULL, written by
+                                rq_subspace_build: 16-bit tags of the bucket's first two key
+                                slots (0 = empty, else 0x8000 for a key in its home bucket or
+                                0x4000 for a key moved on from a full bucket, | the low 13
+                                bits of the key's 32-bit hash), bit 13 of the upper tag set
+                                when slot 2 is occupied too.  The matrix-free kernel probes
+                                these words instead of the key buckets and reads the keys only
+                                where a tag matches or the bucket holds more keys           */
+    int32_t   fpoint;        /* written by rq_subspace_build: pa * 65 + pb when every state has
+                                the same pair pa = popcount(s & fmask_a), pb = popcount(s &
+                                fmask_b) (a subspace in one sector), else -1; -1 with the
+                                filter off                                                  */
 } rq_subspace_t;
 
 typedef struct rq_terms {
@@ -155,6 +167,24 @@ int rq_terms_upload(int32_t J, int32_t K, const uint64_t *xmask, const int32_t *
 /* Fill xhash[j] with the lookup hash of xmask[j] (used by RQ_LOOKUP_HASH matvecs: a row's
  * target bucket is hash(row) ^ xhash[j]).  Setup call, stream-ordered. */
 int rq_terms_hash(const rq_terms_t *terms, uint32_t *xhash, void *stream);
+
+/* Scratch bytes of rq_terms_group for K input terms. */
+int rq_terms_group_scratch_size(int64_t K, size_t *bytes);
+
+/* PauliSumXZ.from_paulisum (rqutils/paulis/symplectic.py:58-125) on the device, for K terms
+ * already parsed into DEVICE arrays xmask[K], zmask[K] (bit q = qubit q, n <= 64) and coef[2K]
+ * (complex128 interleaved), in input order: drops exact-zero coefficients, merges equal strings
+ * (coefficients added from 0 in input order, terms in the lexicographic order of their labels:
+ * character 0 = qubit n-1, I < X < Y < Z), keeps the real parts when force_real, groups by X
+ * mask in ascending order (members in label order) and multiplies each coefficient by
+ * (-i)^(popcount(x & z) mod 4).  Output (device, sized for K): xmask_out[J], toff_out[J + 1]
+ * (int64), zmask_out[K'], coef_out[2K'] (phased); *J_out, *K_out; *flags_out bit 0 = an imaginary
+ * part was dropped under force_real (the reference warns), bit 1 = every phased coefficient is
+ * real.  Synchronises the stream. */
+int rq_terms_group(int64_t K, const uint64_t *xmask, const uint64_t *zmask, const double *coef,
+                   int32_t force_real, uint64_t *xmask_out, int64_t *toff_out,
+                   uint64_t *zmask_out, double *coef_out, int64_t *J_out, int64_t *K_out,
+                   int32_t *flags_out, void *scratch, void *stream);
 
 /* ---- sample front end ------------------------------------------------------------------ */
 
@@ -233,14 +263,18 @@ int rq_lobpcg_solve(const rq_operator_t *op, const rq_lobpcg_params_t *prm, void
                     const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
 
 /* rq_lobpcg_solve without a caller workspace: no counterpart in the reference.  For callers
- * that cannot allocate device memory (a framework-owned allocator such as an XLA custom-call
- * handler, work recorded into a CUDA graph, pre-reserved memory).  The workspace is a static
- * 8 MiB device array of the library, held on every GPU that loads it until the process exits;
- * problems whose rq_lobpcg_workspace_size exceeds 8 MiB are rejected with RQ_E_RANGE (about
- * 60,000 rows in complex128, 40,000 with mixed precision).  Runs without CUDA graphs and
- * allocates nothing.  The first call on a device looks up the array's device address (once per
- * device); make that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU (other streams, other threads) race and must not be issued. */
+ * that cannot allocate device memory: a custom-call handler inside another framework gets only
+ * its operand and result buffers (that framework's pool allocator owns the rest of the device
+ * memory), and a service that reserves its device memory at start-up cannot let a library
+ * cudaMalloc fail or fragment that reserve later.  The workspace is a static 8 MiB device array
+ * of the library, held on every GPU that loads it until the process exits; problems whose
+ * rq_lobpcg_workspace_size exceeds 8 MiB are rejected with RQ_E_RANGE (about 60,000 rows in
+ * complex128, 40,000 with mixed precision).  The call allocates nothing (no cudaMalloc, no
+ * cudaFree, no allocating library routine) and synchronises the stream.  The first call on a
+ * device looks up the array's device address (once per device); make that first call before any
+ * stream capture.  All calls share the array and it keeps the last call's contents (the solver
+ * clears what must start at zero): calls that overlap on the GPU (other streams, other threads)
+ * race and must not be issued. */
 int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_params_t *prm,
                             const void *x0, void *x_out, rq_lobpcg_result_t *res, void *stream);
 

@@ -97,6 +97,85 @@ def matvec_xcached(vec, xsources, terms: OracleTerms, states):
     return out
 
 
+def _group_cuts(terms: OracleTerms):
+    """Number of leading nonzero coefficients of each group: get_diagonal's loop ends at the first
+    zero coefficient (sqd.py:561-564)."""
+    c = np.asarray(terms.c)
+    zero = c == 0
+    first = np.where(zero.any(axis=1), zero.argmax(axis=1), c.shape[1])
+    return first.astype(np.int64)
+
+
+def rows_matvec(vec, terms: OracleTerms, states, rows, chunk=64, halves=None):
+    """apply_h_x_cached (sqd.py:640-654) evaluated on selected rows only, for subspaces too large
+    for the (J, D) table.  For row i and X group j the source is the position of S[i] ^ x_j in the
+    sorted states (searchsorted: the same table as the sort-merge of get_xsource, sqd.py:448-503,
+    which the fixtures check) or absent; the value is sum_j diag_j(S[i]) vec[source], the groups
+    added in ascending order, each diagonal over the group's terms up to its first zero
+    coefficient (sqd.py:554-575).
+
+    ``halves`` = (A, B): optional qubit masks; a target whose (popcount(t & A), popcount(t & B))
+    pair occurs for no state cannot be a state, so it is skipped before the search (an exact
+    shortcut).  Returns (y[rows], hits) with hits a list, per row, of (group, source) pairs in
+    ascending group order over the groups with x != 0."""
+    S = np.asarray(states, dtype=np.uint64)
+    rows = np.asarray(rows, dtype=np.int64)
+    X = np.asarray(terms.x, dtype=np.uint64)
+    Z = np.asarray(terms.z, dtype=np.uint64)
+    C = np.asarray(terms.c)
+    cut = _group_cuts(terms)
+    nz = np.nonzero(X != 0)[0]
+    dg = [int(j) for j in np.nonzero(X == 0)[0]]
+    pairs = None
+    if halves is not None:
+        A, B = (np.uint64(h) for h in halves)
+        pa, pb = np.bitwise_count(S & A).astype(np.int64), np.bitwise_count(S & B).astype(np.int64)
+        pairs = np.unique(pa * 65 + pb)
+    ydt = np.result_type(vec.dtype, C.dtype)
+    y = np.zeros(len(rows), dtype=ydt)
+    hits = []
+
+    def diags(s, groups):
+        if len(groups) == 0:
+            return np.zeros(0, dtype=C.dtype)
+        kc = int(cut[groups].max())
+        zz, cc = Z[groups, :kc], C[groups, :kc]
+        live = np.arange(kc)[None, :] < cut[groups][:, None]
+        sign = 1. - 2. * (np.bitwise_count(zz & s) & np.uint8(1))
+        return np.sum(np.where(live, cc * sign, 0), axis=1)
+
+    for a in range(0, len(rows), chunk):
+        rr = rows[a:a + chunk]
+        t = S[rr][:, None] ^ X[None, nz]                   # (rows, groups with x != 0)
+        if pairs is not None:
+            key = (np.bitwise_count(t & A).astype(np.int64) * 65 +
+                   np.bitwise_count(t & B).astype(np.int64))
+            ri, gi = np.nonzero(np.isin(key, pairs))
+        else:
+            ri, gi = np.nonzero(np.ones(t.shape, dtype=bool))
+        tt = t[ri, gi]
+        pos = np.searchsorted(S, tt)
+        posc = np.minimum(pos, len(S) - 1)
+        found = (pos < len(S)) & (S[posc] == tt)
+        ri, gi, src = ri[found], nz[gi[found]], pos[found]
+        for k, i in enumerate(rr):
+            sel = ri == k
+            g_k, m_k = gi[sel], src[sel]
+            order = np.argsort(g_k, kind='stable')
+            g_k, m_k = g_k[order], m_k[order]
+            hits.append(list(zip(g_k.tolist(), m_k.tolist())))
+            s = S[i]
+            groups = np.array(dg + g_k.tolist(), dtype=np.int64)
+            srcs = np.array([int(i)] * len(dg) + m_k.tolist(), dtype=np.int64)
+            d = diags(s, groups)
+            order = np.argsort(groups, kind='stable')
+            acc = ydt.type(0)
+            for val in (d * vec[srcs])[order]:
+                acc = acc + val
+            y[a + k] = acc
+    return y, hits
+
+
 def matvec_nocache(vec, terms: OracleTerms, states, threads=1):
     """apply_h, sqd.py:590-605: the X sources are recomputed (sort-merge) inside every matvec.
 

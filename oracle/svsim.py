@@ -6,6 +6,10 @@ initial state; per gate out = 1j * sin * signs * state[i ^ x] + cos * state, the
 when cos == 0, signs = (-1)^popcount(i & z)).  The complex products are written out in NumPy's
 own evaluation order so that the device kernel, which rounds each product and sum separately,
 can be compared bit for bit.
+
+Parity pin: ``tests/golden/svsim_*.npz`` hold circuits run through the unmodified reference
+``rqutils/svsim.py`` (``tests/golden/make_golden.py --svsim``, jax replaced by the NumPy stand-in);
+``tests/test_oracle_svsim.py`` checks this restatement against them bit for bit.
 """
 import numpy as np
 

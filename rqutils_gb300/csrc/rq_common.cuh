@@ -202,6 +202,34 @@ struct KeyWidth<32> {
     }
 };
 
+// Tag words (rq_subspace_t.htags), one 32-bit word per bucket: the 16-bit tags of slots 0 (low
+// half) and 1 (high half), 0 for an empty slot; bit 29 (bit 13 of slot 1's tag) is set when slot 2
+// is occupied as well.  Half a key per bucket on average: 1.4 % of buckets hold three or more.
+constexpr uint32_t kTagHome = 0x8000u;   // key stored in its home bucket
+constexpr uint32_t kTagMoved = 0x4000u;  // key moved on from a full bucket
+constexpr uint32_t kTagMask = 0x1FFFu;   // low bits of the key's hash
+constexpr uint32_t kTagMore = 0x20000000u;
+
+// One bucket's tag word in a single 32-bit read-only load; 0 (no tags) when pred is false.
+__device__ __forceinline__ uint32_t load_tags(const uint32_t *p, bool pred) {
+    uint32_t w = 0u;
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t"
+        "@q ld.global.nc.u32 %0, [%1];\n\t}"
+        : "+r"(w)
+        : "l"(p), "r"((unsigned)pred));
+    return w;
+}
+
+// Tag test of target hash h against a tag word: hot when slot 0 or 1 holds a home-bucket key with
+// h's tag (a zero 16-bit lane of the word ^ tag, found with the borrow test (v - 1) & ~v & 0x8000
+// per lane, which is exact for "some lane is zero") or when the bucket holds more keys than the
+// word shows.  The word 0 (no keys, or a probe that was skipped) is never hot.
+__device__ __forceinline__ bool tags_hot(uint32_t w, uint32_t h) {
+    const uint32_t rep = (kTagHome | (h & kTagMask)) * 0x00010001u;
+    const uint32_t v = (w & ~kTagMore) ^ rep;
+    return (((v - 0x00010001u) & ~v & 0x80008000u) | (w & kTagMore)) != 0u;
+}
+
 // Branch-free bucket test: `any` when a slot equals t, `open` when the last slot is empty.
 template <typename Bk, typename K>
 __device__ __forceinline__ void test_bucket(const Bk &b, K t, K e, bool &any, bool &open) {

@@ -1726,12 +1726,12 @@ namespace rq {
 // Allocation-free solve
 // ------------------------------------------------------------------------------------------
 // For callers that must not allocate device memory themselves -- code running inside a
-// framework that owns the allocator (an XLA custom-call handler gets only its operand and
-// result buffers), code recorded into a CUDA graph (no allocation while a stream is being
-// captured) or a process whose memory is reserved up front.  The solver's workspace (reduction
-// partials and counters, the matvec's error record, the iteration vectors) lives in this
-// file-scope device array instead of caller memory.  Every GPU that loads the library holds it
-// until the process exits.
+// framework that owns the allocator (a custom-call handler gets only its operand and result
+// buffers; the framework's pool holds the rest of the memory) or a service whose device memory is
+// reserved up front (a later cudaMalloc could fail or fragment the reserve).  The solver's
+// workspace (reduction partials and counters, the matvec's error record, the iteration vectors)
+// lives in this file-scope device array instead of caller memory.  Every GPU that loads the
+// library holds it until the process exits.
 namespace {
 
 constexpr size_t kNoallocBytes = size_t(8) << 20;  // 8 MiB
@@ -1777,8 +1777,9 @@ RQ_API int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_para
                         std::to_string(kNoallocBytes) + " bytes (use rq_lobpcg_solve)");
     void *ws = nullptr;
     RQ_TRY(noalloc_workspace(&ws));
-    // No graph: instantiating one may allocate device memory.  The workspace carries the last
-    // call's contents; solve() clears the reduction counter and the error record it relies on.
+    // No CUDA graph of its own: instantiating one may allocate device memory.  The workspace
+    // carries the last call's contents; solve() clears the reduction counter and the error
+    // record it relies on.
     rq_lobpcg_params_t p = *prm;
     p.use_graph = 0;
     return solve_entry(op, nullptr, nullptr, &p, ws, x0, x_out, res, stream);

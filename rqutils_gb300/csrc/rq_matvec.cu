@@ -183,28 +183,69 @@ __shared__ uint32_t hk_fb[RQ_FILTER_WORDS];
 __shared__ uint32_t hk_htab[kHashTableWords];
 extern __shared__ __align__(16) unsigned char hk_dyn[];
 
+// Group keys of resident indices [c0, c0 + cn) into shared-memory slots [0, cn); the layout holds
+// kt slots (32-bit keys: (x, h(x)) pairs; 64-bit keys: x masks, then hashes).  Resident index c is
+// group c + (c >= diag_group).  All threads of the block call it.
+template <int KB>
+__device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int cn, int kt) {
+    constexpr int NB = KeyWidth<KB>::kNbytes;
+    const int skip = T.diag_group;
+    for (int c = threadIdx.x; c < cn; c += blockDim.x) {
+        const int j = c0 + c + (skip >= 0 && c0 + c >= skip);
+        const uint64_t xv = T.xmask[j];
+        const uint32_t h = T.xhash ? T.xhash[j] : lin_hash(hk_htab, xv, NB);
+        if (KB == 32) {
+            reinterpret_cast<uint2 *>(hk_dyn)[c] = make_uint2((uint32_t)xv, h);
+        } else {
+            reinterpret_cast<uint64_t *>(hk_dyn)[c] = xv;
+            reinterpret_cast<uint32_t *>(hk_dyn + align16((size_t)kt * 8))[c] = h;
+        }
+    }
+}
+
+// Probes in flight per thread: four with key buckets (a 16- or 32-byte bucket per probe fills the
+// 40 registers of six resident 256-thread blocks), eight with tag words (one register per probe)
+// where that fits the registers without spills (ptxas -v): 32-bit keys without the bitset
+// filter.  A divisor of the 64 groups of a super-chunk.
+#ifndef RQ_TAG_PROBES
+#define RQ_TAG_PROBES 8
+#endif
+constexpr int kKeyProbes = 4;
+
 template <typename V, int KB, int FM>
+constexpr int tag_probes() {
+    return (FM == kFiltSet || KB == 64) ? 4 : RQ_TAG_PROBES;
+}
+
+// TL: the group keys may need streaming in tiles (1024-thread kernels only; with 256-thread blocks
+// they always fit and the tile loop is one pass known at compile time).
+template <typename V, int KB, int FM, bool TG, bool TL>
 __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__restrict__ x,
                                           V *__restrict__ y, int *err, int pa0, int pb0) {
     using R = typename VT<V>::R;
     using K = typename KeyWidth<KB>::K;
     constexpr int NB = KeyWidth<KB>::kNbytes;
     constexpr int kBucketBytes = KeyWidth<KB>::kBucketBytes;
-    constexpr int U = 4;  // probes in flight per thread (no spills at 40 registers)
+    constexpr int U = TG ? tag_probes<V, KB, FM>() : kKeyProbes;
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
     const int64_t D = S.D;
     const int skip = T.diag_group;  // the x = 0 group is applied outside the probe loop
-    const int nres = T.J - (skip >= 0 ? 1 : 0);  // resident groups
+    const int nres = T.J - (skip >= 0 ? 1 : 0);  // groups of the probe loop
+    // shared-memory slots: every group's keys when they fit (loaded once by the kernel), else
+    // tiles of kMaxResidentGroups streamed through for every row batch
+    const int kt = (!TL || nres <= kMaxResidentGroups) ? nres : kMaxResidentGroups;
+    const bool tiled = TL && nres > kt;
     const uint2 *gk32 = reinterpret_cast<const uint2 *>(hk_dyn);
     const uint64_t *gx64 = reinterpret_cast<const uint64_t *>(hk_dyn);
-    const uint32_t *gh64 = reinterpret_cast<const uint32_t *>(hk_dyn + align16((size_t)T.J * 8));
+    const uint32_t *gh64 = reinterpret_cast<const uint32_t *>(hk_dyn + align16((size_t)kt * 8));
     const bool d0 = (op.diag0 != nullptr) && (skip >= 0);
     const K fa = (K)S.fmask_a, fbm = (K)S.fmask_b, empty = (K)S.empty_key;
     const int shift = 32 - S.hbits;
     const uint32_t *pmap = S.pbits > 0 ? S.pmap : nullptr;
     const int pshift = 32 - S.pbits;
     const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
+    const uint32_t *tags = S.htags;
     auto sector = [&](K t) -> bool {
         if (FM == kFiltPoint) {
             int pa, pb;
@@ -240,117 +281,114 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
         } else if (skip >= 0) {
             acc.add(cmul(group_diag<R>(T, skip, s64), xi));
         }
-        for (int gs0 = 0; gs0 < nres; gs0 += 64) {
-            const int gs1 = min(nres, gs0 + 64);
-            uint64_t hot = 0ULL;
-            int g = gs0;
-            for (; g + U <= gs1; g += U) {
-                K t[U];
-                uint32_t b[U];
-                bool q[U];
-                typename KeyWidth<KB>::Bucket w[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    uint32_t hxg;
-                    if (KB == 32) {
-                        const uint2 e = gk32[g + u];
-                        t[u] = s ^ (K)e.x;
-                        hxg = e.y;
-                    } else {
-                        t[u] = s ^ (K)gx64[g + u];
-                        hxg = gh64[g + u];
-                    }
-                    q[u] = sector(t[u]);
-                    b[u] = hs ^ hxg;
-                }
-                if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
-                    uint32_t pw[U];
+        for (int t0 = 0; TL ? t0 < nres : t0 < 1; t0 += TL ? kt : 1) {
+            const int tn = TL ? min(kt, nres - t0) : nres;
+            if (tiled) {
+                __syncthreads();  // the previous tile is no longer read
+                load_group_keys<KB>(T, t0, tn, kt);
+                __syncthreads();
+            }
+            for (int gs0 = 0; gs0 < tn; gs0 += 64) {
+                const int gs1 = min(tn, gs0 + 64);
+                uint64_t hot = 0ULL;
+                int g = gs0;
+                for (; g + U <= gs1; g += U) {
+                    K t[U];
+                    uint32_t b[U];
+                    bool q[U];
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
-                        const uint32_t idx = b[u] >> pshift;
-                        pw[u] = q[u] ? __ldg(pmap + (idx >> 5)) : 0u;
+                        uint32_t hxg;
+                        if (KB == 32) {
+                            const uint2 e = gk32[g + u];
+                            t[u] = s ^ (K)e.x;
+                            hxg = e.y;
+                        } else {
+                            t[u] = s ^ (K)gx64[g + u];
+                            hxg = gh64[g + u];
+                        }
+                        q[u] = sector(t[u]);
+                        b[u] = hs ^ hxg;
                     }
+                    if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
+                        uint32_t pw[U];
 #pragma unroll
-                    for (int u = 0; u < U; ++u) q[u] = q[u] && ((pw[u] >> ((b[u] >> pshift) & 31)) & 1u);
+                        for (int u = 0; u < U; ++u) {
+                            const uint32_t idx = b[u] >> pshift;
+                            pw[u] = q[u] ? __ldg(pmap + (idx >> 5)) : 0u;
+                        }
+#pragma unroll
+                        for (int u = 0; u < U; ++u) q[u] = q[u] && ((pw[u] >> ((b[u] >> pshift) & 31)) & 1u);
+                    }
+                    uint32_t hb = 0u;  // hot bits of this batch, constant shifts
+                    if (TG) {
+                        // tag words: a hot lane has a home-bucket tag equal to its target's or a
+                        // bucket with more keys than the word shows (the resolution below compares
+                        // the keys).  A lane whose target fails the filter reads no word: the zero
+                        // word it keeps is never hot, so q need not stay live across the loads.
+                        uint32_t w[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) w[u] = load_tags(tags + (b[u] >> shift), q[u]);
+#pragma unroll
+                        for (int u = 0; u < U; ++u)
+                            if (tags_hot(w[u], b[u])) hb |= 1u << u;
+                    } else {
+                        typename KeyWidth<KB>::Bucket w[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u)
+                            w[u] = KeyWidth<KB>::load(keys + (size_t)(b[u] >> shift) * kBucketBytes,
+                                                      q[u], S.empty_key);
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            bool any, open;
+                            test_bucket(w[u], t[u], empty, any, open);
+                            if (q[u] && (any || !open)) hb |= 1u << u;
+                        }
+                    }
+                    hot |= (uint64_t)hb << (g - gs0);
                 }
-#pragma unroll
-                for (int u = 0; u < U; ++u)
-                    w[u] = KeyWidth<KB>::load(keys + (size_t)(b[u] >> shift) * kBucketBytes, q[u],
-                                              S.empty_key);
-                uint32_t hb = 0u;  // hot bits of this batch, constant shifts
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    bool any, open;
-                    test_bucket(w[u], t[u], empty, any, open);
-                    if (q[u] && (any || !open)) hb |= 1u << u;
+                for (; g < gs1; ++g) {  // tail: mark and resolve below
+                    const K t = s ^ (KB == 32 ? (K)gk32[g].x : (K)gx64[g]);
+                    if (sector(t)) hot |= 1ULL << (g - gs0);
                 }
-                hot |= (uint64_t)hb << (g - gs0);
+                while (hot) {
+                    const int gc = gs0 + __ffsll((long long)hot) - 1;  // slot in shared memory
+                    hot &= hot - 1ULL;
+                    const int gr = t0 + gc;                             // index among the groups
+                    const int gg = gr + (skip >= 0 && gr >= skip);
+                    const uint64_t xv = __ldg(T.xmask + gg);
+                    const uint32_t hxg = KB == 32 ? gk32[gc].y : gh64[gc];
+                    const int m = lookup_hash_at<KB>(S, s64 ^ xv, (hs ^ hxg) >> shift, err);
+                    if (m >= 0) acc.add(cmul(group_diag<R>(T, gg, s64), VT<V>::ld(x, m)));
+                }
+                __syncwarp();
             }
-            for (; g < gs1; ++g) {  // tail: mark and resolve below
-                const K t = s ^ (KB == 32 ? (K)gk32[g].x : (K)gx64[g]);
-                if (sector(t)) hot |= 1ULL << (g - gs0);
-            }
-            while (hot) {
-                const int gc = gs0 + __ffsll((long long)hot) - 1;
-                hot &= hot - 1ULL;
-                const int gg = gc + (skip >= 0 && gc >= skip);
-                const uint64_t xv = __ldg(T.xmask + gg);
-                const uint32_t hxg = KB == 32 ? gk32[gc].y : gh64[gc];
-                const int m = lookup_hash_at<KB>(S, s64 ^ xv, (hs ^ hxg) >> shift, err);
-                if (m >= 0) acc.add(cmul(group_diag<R>(T, gg, s64), VT<V>::ld(x, m)));
-            }
-            __syncwarp();
         }
         if (active) VT<V>::st(y, i, acc.get());
     }
 }
 
-template <typename V, int KB, bool FILTER, int BLOCK>
+// FM: the sector filter's form, chosen on the host from rq_subspace_t.fpoint (one kernel per
+// form, so that the registers of the general bitset test do not weigh on the one-sector kernel)
+template <typename V, int KB, int FM, int BLOCK, bool TG>
 __global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : (sizeof(V) <= 8 ? 6 : 4))
 k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int *err,
               const int *gate, const int *gate2) {
     constexpr int NB = KeyWidth<KB>::kNbytes;
     if (gate && (*gate == 0 || (gate2 && *gate2 == 0))) return;
-    __shared__ int s_fcount, s_fbit;
-    unsigned char *smem = hk_dyn;
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
-    const int J = T.J;
-    const int skip = T.diag_group;
-    uint32_t *htab = hk_htab;
-    if (threadIdx.x == 0) {
-        s_fcount = 0;
-        s_fbit = 0;
-    }
-    init_hash_tables(htab, NB);
+    init_hash_tables(hk_htab, NB);
+    if (FM == kFiltSet)
+        for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) hk_fb[w] = S.fbits[w];
     __syncthreads();
-    for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) {
-        const uint32_t v = S.fbits[w];
-        hk_fb[w] = v;
-        if (FILTER && v) {
-            atomicAdd(&s_fcount, __popc(v));
-            atomicMax(&s_fbit, w * 32 + 31 - __clz(v));
-        }
-    }
-    for (int j = threadIdx.x; j < J; j += blockDim.x) {
-        if (j == skip) continue;
-        const int r = j - (skip >= 0 && j > skip);
-        const uint64_t xv = T.xmask[j];
-        const uint32_t h = T.xhash ? T.xhash[j] : lin_hash(htab, xv, NB);
-        if (KB == 32) {
-            reinterpret_cast<uint2 *>(smem)[r] = make_uint2((uint32_t)xv, h);
-        } else {
-            reinterpret_cast<uint64_t *>(smem)[r] = xv;
-            reinterpret_cast<uint32_t *>(smem + align16((size_t)J * 8))[r] = h;
-        }
-    }
+    const int nres = T.J - (T.diag_group >= 0 ? 1 : 0);
+    if (nres <= kMaxResidentGroups) load_group_keys<KB>(T, 0, nres, nres);  // else in tiles
     __syncthreads();
-    if (!FILTER)
-        hash_rows<V, KB, kFiltNone>(op, x, y, err, 0, 0);
-    else if (s_fcount == 1)
-        hash_rows<V, KB, kFiltPoint>(op, x, y, err, s_fbit / 65, s_fbit % 65);
+    if (FM == kFiltPoint)
+        hash_rows<V, KB, FM, TG, BLOCK == 1024>(op, x, y, err, S.fpoint / 65, S.fpoint % 65);
     else
-        hash_rows<V, KB, kFiltSet>(op, x, y, err, 0, 0);
+        hash_rows<V, KB, FM, TG, BLOCK == 1024>(op, x, y, err, 0, 0);
 }
 
 // xhash[j] = h(xmask[j])
@@ -629,11 +667,12 @@ int prepare_launch(KernT kern, size_t smem, size_t &configured, size_t &occ_smem
     return RQ_OK;
 }
 
-template <typename V, int KB, bool FILTER, int BLOCK>
+template <typename V, int KB, int FM, int BLOCK, bool TG>
 int launch_hash_block(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
                       const int *gate, const int *gate2) {
-    auto kern = k_matvec_hash<V, KB, FILTER, BLOCK>;
-    const size_t smem = group_key_bytes<KB>(op.terms.J);
+    auto kern = k_matvec_hash<V, KB, FM, BLOCK, TG>;
+    const int nres = op.terms.J - (op.terms.diag_group >= 0 ? 1 : 0);
+    const size_t smem = group_key_bytes<KB>(nres < kMaxResidentGroups ? nres : kMaxResidentGroups);
     static size_t configured = 0, occ_smem = ~size_t(0);
     static int occ_blocks = 1;
     if (smem > 48 * 1024 && smem > configured) {
@@ -655,15 +694,19 @@ int launch_hash_block(const rq_operator_t &op, const void *x, void *y, int *err,
     return RQ_OK;
 }
 
-template <typename V, int KB, bool FILTER>
+template <typename V, int KB, int FM>
 int launch_hash(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
                 const int *gate, const int *gate2) {
-    if (op.terms.J > kMaxResidentGroups)
-        return fail(RQ_E_RANGE, "rq_matvec: more than 16384 X groups for the hash kernel");
-    // small group sets: several 256-thread blocks per SM; large ones: one 1024-thread block
-    if (group_key_bytes<KB>(op.terms.J) <= 16 * 1024)
-        return launch_hash_block<V, KB, FILTER, 256>(op, x, y, err, st, gate, gate2);
-    return launch_hash_block<V, KB, FILTER, 1024>(op, x, y, err, st, gate, gate2);
+    // small group sets: several 256-thread blocks per SM; large ones (streamed in tiles of
+    // kMaxResidentGroups above that count): one 1024-thread block.
+    // With the tag words the probes read 4 bytes per bucket (not with 64-bit keys and the bitset
+    // filter, whose tag kernel spills registers).
+    const bool small = op.terms.J <= kMaxResidentGroups && group_key_bytes<KB>(op.terms.J) <= 16 * 1024;
+    if (op.sub.htags && !(KB == 64 && FM == kFiltSet))
+        return small ? launch_hash_block<V, KB, FM, 256, true>(op, x, y, err, st, gate, gate2)
+                     : launch_hash_block<V, KB, FM, 1024, true>(op, x, y, err, st, gate, gate2);
+    return small ? launch_hash_block<V, KB, FM, 256, false>(op, x, y, err, st, gate, gate2)
+                 : launch_hash_block<V, KB, FM, 1024, false>(op, x, y, err, st, gate, gate2);
 }
 
 template <typename V, int LK>
@@ -714,13 +757,19 @@ int matvec_typed(const rq_operator_t &op, const void *x, void *y, void *scratch,
     switch (op.mode) {
         case RQ_MODE_FREE:
             if (op.sub.lookup == RQ_LOOKUP_HASH) {
-                // the sector filter is off when both masks are zero
-                const bool filt = (op.sub.fmask_a | op.sub.fmask_b) != 0;
-                if (op.sub.key_bits == 32)
-                    return filt ? launch_hash<V, 32, true>(op, x, y, err, st, gate, gate2)
-                                : launch_hash<V, 32, false>(op, x, y, err, st, gate, gate2);
-                return filt ? launch_hash<V, 64, true>(op, x, y, err, st, gate, gate2)
-                            : launch_hash<V, 64, false>(op, x, y, err, st, gate, gate2);
+                // the sector filter is off when both masks are zero; a subspace in one sector
+                // (fpoint >= 0) tests two popcounts instead of the bitset
+                const int fm = (op.sub.fmask_a | op.sub.fmask_b) == 0 ? kFiltNone
+                               : op.sub.fpoint >= 0                     ? kFiltPoint
+                                                                        : kFiltSet;
+                if (op.sub.key_bits == 32) {
+                    if (fm == kFiltPoint) return launch_hash<V, 32, kFiltPoint>(op, x, y, err, st, gate, gate2);
+                    if (fm == kFiltSet) return launch_hash<V, 32, kFiltSet>(op, x, y, err, st, gate, gate2);
+                    return launch_hash<V, 32, kFiltNone>(op, x, y, err, st, gate, gate2);
+                }
+                if (fm == kFiltPoint) return launch_hash<V, 64, kFiltPoint>(op, x, y, err, st, gate, gate2);
+                if (fm == kFiltSet) return launch_hash<V, 64, kFiltSet>(op, x, y, err, st, gate, gate2);
+                return launch_hash<V, 64, kFiltNone>(op, x, y, err, st, gate, gate2);
             }
             if (op.sub.lookup == RQ_LOOKUP_BSEARCH)
                 return launch_free<V, RQ_LOOKUP_BSEARCH>(op, x, y, 1, err, st, gate, gate2);

@@ -102,6 +102,82 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(const uint64_t *__rest
     }
 }
 
+// The same two passes for a permutation: element i stands for index perm[i], its digit is taken
+// from key[perm[i]], and the scatter moves the index (a stable sort of the indices by the key).
+__global__ void __launch_bounds__(kSortThreads) k_hist_perm(const uint64_t *__restrict__ key,
+                                                            const int64_t *__restrict__ perm, int64_t n,
+                                                            int shift, int64_t tiles,
+                                                            int64_t *__restrict__ counts) {
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t t0 = (int64_t)blockIdx.x * kTile;
+    for (int r = 0; r < kRounds; ++r) {
+        const int64_t i = t0 + (int64_t)r * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(int)((key[perm[i]] >> shift) & 255ULL)], 1);
+    }
+    __syncthreads();
+    counts[1 + (int64_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter_perm(const uint64_t *__restrict__ key,
+                                                               const int64_t *__restrict__ src,
+                                                               int64_t *__restrict__ dst, int64_t n,
+                                                               int shift, int64_t tiles,
+                                                               const int64_t *__restrict__ base) {
+    __shared__ unsigned long long run[256];
+    __shared__ int wcnt[kSortThreads / 32][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    run[tid] = (unsigned long long)base[(int64_t)tid * tiles + blockIdx.x];
+    for (int w = 0; w < kSortThreads / 32; ++w) wcnt[w][tid] = 0;
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t t0 = (int64_t)blockIdx.x * kTile;
+    for (int r = 0; r < kRounds; ++r) {
+        const int64_t i = t0 + (int64_t)r * kSortThreads + tid;
+        const bool valid = i < n;
+        const int64_t e = valid ? src[i] : 0;
+        const int d = valid ? (int)((key[e] >> shift) & 255ULL) : 256;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & lt);
+        const bool leader = (__ffs(peers) - 1) == lane;
+        if (valid && leader) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            unsigned long long pos = run[d] + (unsigned long long)rank;
+            for (int w = 0; w < warp; ++w) pos += (unsigned long long)wcnt[w][d];
+            dst[pos] = e;
+        }
+        __syncthreads();
+        if (valid && leader) {
+            atomicAdd(&run[d], (unsigned long long)__popc(peers));
+            wcnt[warp][d] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_iota64(int64_t *p, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = i;
+}
+
+__global__ void k_or_and_perm(const uint64_t *__restrict__ k, int64_t n, unsigned long long *oa) {
+    unsigned long long o = 0ULL, a = ~0ULL;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        o |= k[i];
+        a &= k[i];
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        o |= __shfl_xor_sync(0xffffffffu, o, s);
+        a &= __shfl_xor_sync(0xffffffffu, a, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicOr(oa, o);
+        atomicAnd(oa + 1, a);
+    }
+}
+
 __global__ void k_flags(const uint64_t *__restrict__ s, int64_t n, int64_t *__restrict__ fl) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         fl[i] = (i == 0 || s[i] != s[i - 1]) ? 1 : 0;
@@ -145,6 +221,60 @@ int grid_for(int64_t n) {
 }
 
 }  // namespace
+
+// Stable sort of the indices 0..n-1 by a key of nw 64-bit words (words[0] the least significant),
+// left in perm; least-significant-digit passes over the 8-bit digits on which the keys differ.
+// Scratch: alt [n], counts [256 * tiles + 1], bsum (scan block sums), oa [2] words.
+size_t sort_perm_scratch(int64_t n) {
+    const int64_t tiles = tiles_of(n);
+    const int64_t ncnt = 256 * tiles + 1;
+    return ((size_t)n * 8 + 255) / 256 * 256 + ((size_t)ncnt * 8 + 255) / 256 * 256 +
+           ((size_t)((ncnt + 1023) / 1024 + 1) * 8 + 255) / 256 * 256 + 256;
+}
+
+int sort_perm(const uint64_t *const *words, int nw, int64_t n, int64_t *perm, void *scratch,
+              cudaStream_t st) {
+    if (n < 1) return RQ_OK;
+    const int64_t tiles = tiles_of(n);
+    const int64_t ncnt = 256 * tiles + 1;
+    char *w = static_cast<char *>(scratch);
+    int64_t *alt = reinterpret_cast<int64_t *>(w);
+    w += ((size_t)n * 8 + 255) / 256 * 256;
+    int64_t *counts = reinterpret_cast<int64_t *>(w);
+    w += ((size_t)ncnt * 8 + 255) / 256 * 256;
+    int64_t *bsum = reinterpret_cast<int64_t *>(w);
+    w += ((size_t)((ncnt + 1023) / 1024 + 1) * 8 + 255) / 256 * 256;
+    unsigned long long *oa = reinterpret_cast<unsigned long long *>(w);
+    k_iota64<<<grid_for(n), kThreads, 0, st>>>(perm, n);
+    RQ_CUDA(cudaGetLastError());
+    int64_t *bufs[2] = {perm, alt};
+    int cur = 0;
+    for (int k = 0; k < nw; ++k) {
+        const unsigned long long init[2] = {0ULL, ~0ULL};
+        RQ_CUDA(cudaMemcpyAsync(oa, init, sizeof(init), cudaMemcpyHostToDevice, st));
+        k_or_and_perm<<<grid_for(n), kThreads, 0, st>>>(words[k], n, oa);
+        unsigned long long h_oa[2];
+        RQ_CUDA(cudaMemcpyAsync(h_oa, oa, sizeof(h_oa), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaStreamSynchronize(st));
+        const uint64_t vary = h_oa[0] ^ h_oa[1];
+        for (int p = 0; p < 8; ++p) {
+            if (!((vary >> (8 * p)) & 0xFFULL)) continue;
+            RQ_CUDA(cudaMemsetAsync(counts, 0, sizeof(int64_t), st));
+            k_hist_perm<<<(unsigned)tiles, kSortThreads, 0, st>>>(words[k], bufs[cur], n, 8 * p,
+                                                                  tiles, counts);
+            RQ_CUDA(cudaGetLastError());
+            RQ_TRY(scan_row_counts(counts + 1, 256 * tiles, bsum, st));
+            k_scatter_perm<<<(unsigned)tiles, kSortThreads, 0, st>>>(words[k], bufs[cur],
+                                                                     bufs[cur ^ 1], n, 8 * p,
+                                                                     tiles, counts);
+            RQ_CUDA(cudaGetLastError());
+            cur ^= 1;
+        }
+    }
+    if (cur) RQ_CUDA(cudaMemcpyAsync(perm, alt, (size_t)n * 8, cudaMemcpyDeviceToDevice, st));
+    return RQ_OK;
+}
+
 }  // namespace rq
 
 using namespace rq;

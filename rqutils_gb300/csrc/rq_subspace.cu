@@ -92,6 +92,36 @@ k_hash_insert(const uint64_t *__restrict__ states, int64_t D, void *keys, int32_
     }
 }
 
+// Tag word of each bucket, one thread per bucket: the tags of slots 0 and 1 (0 for an empty slot,
+// else 0x8000 for a key in its home bucket or 0x4000 for a key moved on from a full bucket, | the
+// low 13 bits of the key's hash) and the "more keys" bit when slot 2 is occupied.  A probe compares
+// its target's tag with the word and reads the keys only when it matches or has more keys.
+template <int KB>
+__global__ void __launch_bounds__(kThreads)
+k_tag_fill(const void *__restrict__ keys, int hbits, uint64_t empty, uint32_t *__restrict__ tags) {
+    using K = typename KeyWidth<KB>::K;
+    __shared__ uint32_t T[kHashTableWords];
+    init_hash_tables(T, KeyWidth<KB>::kNbytes);
+    __syncthreads();
+    const int64_t nb = int64_t(1) << hbits;
+    const K *kk = static_cast<const K *>(keys);
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t w = 0u;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const K k = kk[b * kBucketSlots + s];
+            if (k == (K)empty) continue;
+            const uint32_t h = lin_hash(T, (uint64_t)k, KeyWidth<KB>::kNbytes);
+            const uint32_t home = bucket_from_hash(h, hbits);
+            const uint32_t tag = (home == (uint32_t)b ? kTagHome : kTagMoved) | (h & kTagMask);
+            w |= tag << (16 * s);
+        }
+        if (kk[b * kBucketSlots + 2] != (K)empty) w |= kTagMore;
+        tags[b] = w;
+    }
+}
+
 __global__ void k_fill_u32(uint32_t *p, int64_t n, uint32_t v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -313,11 +343,31 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
                                    sub->hkeys, sub->hvals, sub->hbits, &sub->empty_key, flag, gap,
                                    st, sub->pbits ? sub->pmap : nullptr, sub->pbits);
     if (rc != RQ_OK) return fail(rc, std::string("rq_subspace_build: ") + rq_last_error());
+    if (sub->lookup == RQ_LOOKUP_HASH && sub->htags) {
+        const int g = grid_for(int64_t(1) << sub->hbits);
+        uint32_t *tags = sub->htags;
+        if (sub->key_bits == 64)
+            k_tag_fill<64><<<g, kThreads, 0, st>>>(sub->hkeys, sub->hbits, sub->empty_key, tags);
+        else
+            k_tag_fill<32><<<g, kThreads, 0, st>>>(sub->hkeys, sub->hbits, sub->empty_key, tags);
+        RQ_CUDA(cudaGetLastError());
+    }
     RQ_CUDA(cudaMemsetAsync(sub->fbits, 0, RQ_FILTER_WORDS * sizeof(uint32_t), st));
     k_filter_build<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->fmask_a, sub->fmask_b,
                                                       sub->fbits);
     RQ_CUDA(cudaGetLastError());
+    // one sector (a single bit of the bitset): the matrix-free kernel then tests two popcounts
+    uint32_t fb[RQ_FILTER_WORDS];
+    RQ_CUDA(cudaMemcpyAsync(fb, sub->fbits, sizeof(fb), cudaMemcpyDeviceToHost, st));
     RQ_CUDA(cudaStreamSynchronize(st));
+    int nbits = 0, bit = -1;
+    for (int w = 0; w < RQ_FILTER_WORDS; ++w)
+        for (int k = 0; k < 32; ++k)
+            if ((fb[w] >> k) & 1u) {
+                ++nbits;
+                bit = w * 32 + k;
+            }
+    sub->fpoint = ((sub->fmask_a | sub->fmask_b) != 0 && nbits == 1) ? bit : -1;
     return RQ_OK;
 }
 

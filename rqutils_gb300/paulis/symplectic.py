@@ -103,10 +103,16 @@ class PauliSumXZ:
 
     # ------------------------------------------------------------------------------------------
     @classmethod
-    def from_paulisum(cls, paulisum, force_real=False, add_padding=False):
+    def from_paulisum(cls, paulisum, force_real=False, add_padding=False, device=None):
         """symplectic.py:51-125: parse ``([str], [coeff])`` or a qiskit ``SparsePauliOp``;
         consolidate (drop exact zeros, merge duplicate strings in lexicographic order); group by X
-        signature in ascending order; phase by (-i)^{popcount(x & z) mod 4}; real when possible."""
+        signature in ascending order; phase by (-i)^{popcount(x & z) mod 4}; real when possible.
+
+        ``device`` (not in the reference): a CUDA device on which the consolidation, grouping
+        and phasing run (``rq_terms_group``); the labels are parsed into X / Z masks on the host.
+        The result is the same, bit for bit."""
+        if device is not None and isinstance(paulisum, tuple):
+            return cls._from_paulisum_device(paulisum, force_real, add_padding, device)
         if isinstance(paulisum, tuple):
             paulis, coeffs = paulisum
             if len(paulis) != len(coeffs):
@@ -156,6 +162,57 @@ class PauliSumXZ:
         if np.all(phc.imag == 0.):
             phc = phc.real.copy()
         return cls._from_compact(xuniq, toff, zsig, phc, n, add_padding)
+
+    @classmethod
+    def _from_paulisum_device(cls, paulisum, force_real, add_padding, device):
+        """The (labels, coeffs) form of from_paulisum with rq_terms_group doing the array work."""
+        import ctypes
+        import torch
+        from .. import _lib as L
+        paulis, coeffs = paulisum
+        if len(paulis) != len(coeffs):
+            raise ValueError('Lengths of Pauli and coeff lists do not match')
+        if len(set(len(p) for p in paulis)) != 1:
+            raise ValueError('Pauli strings have non-uniform lengths')
+        n = len(paulis[0])
+        if n > 64:
+            raise ValueError('at most 64 qubits are supported')
+        labels = np.array([p.upper() for p in paulis], dtype=f'<U{max(n, 1)}')
+        codes = labels.view(np.uint32).reshape(len(labels), n) if n else np.zeros((len(labels), 0))
+        xm = bits_to_masks((codes == ord('X')) | (codes == ord('Y')))
+        zm = bits_to_masks((codes == ord('Y')) | (codes == ord('Z')))
+        c_in = np.array(coeffs)
+        K = len(labels)
+        dev = torch.device(device)
+
+        def u64(a):
+            return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).to(dev)
+
+        cin = torch.from_numpy(np.ascontiguousarray(c_in, dtype=np.complex128)).to(dev)
+        d_x, d_z = u64(xm), u64(zm)
+        xo = torch.empty(K, dtype=torch.int64, device=dev)
+        to = torch.empty(K + 1, dtype=torch.int64, device=dev)
+        zo = torch.empty(K, dtype=torch.int64, device=dev)
+        co = torch.empty(K, dtype=torch.complex128, device=dev)
+        nb = ctypes.c_size_t()
+        L.check(L.lib().rq_terms_group_scratch_size(K, ctypes.byref(nb)), 'rq_terms_group')
+        scratch = torch.empty(int(nb.value), dtype=torch.uint8, device=dev)
+        J, K2, flags = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        with torch.cuda.device(dev):
+            L.check(L.lib().rq_terms_group(K, L.ptr(d_x), L.ptr(d_z), L.ptr(cin),
+                                           int(bool(force_real)), L.ptr(xo), L.ptr(to), L.ptr(zo),
+                                           L.ptr(co), ctypes.byref(J), ctypes.byref(K2),
+                                           ctypes.byref(flags), L.ptr(scratch), L.stream_ptr()),
+                    'rq_terms_group')
+        J, K2 = J.value, K2.value
+        if flags.value & 1:
+            warnings.warn('Found nonzero imaginary part when force_real=True')
+        coef = co[:K2].cpu().numpy()
+        if flags.value & 2:
+            coef = coef.real.copy()
+        return cls._from_compact(xo[:J].cpu().numpy().view(np.uint64),
+                                 to[:J + 1].cpu().numpy(), zo[:K2].cpu().numpy().view(np.uint64),
+                                 coef, n, add_padding)
 
     # ------------------------------------------------------------------------------------------
     @property

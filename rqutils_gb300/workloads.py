@@ -375,6 +375,48 @@ def _enumerate_sector(blocks):
     return np.sort(out)
 
 
+class BenchmarkProblem:
+    """One benchmark configuration: the Pauli sum, the sorted subspace and the seeded input vector.
+
+    ``name``: ``hubbard`` (Fermi-Hubbard 4x4 periodic, t = 1, U = 4, 32 spin-orbitals; D = 2^20
+    drawn from the 8-up / 8-down sector, seed 1; complex64), ``chemistry`` (32 spatial orbitals ->
+    64 spin-orbitals, the 50,000 largest |c|; D = 2^26 at 16 alpha + 16 beta, seed 5; complex64) or
+    ``random20`` (20 qubits, K = 200 terms of locality 1..4, N(0, 1) coefficients; D = 16384 at
+    Hamming weight 10, seed 20; complex128).  ``rows`` overrides D (smaller profiling cases)."""
+
+    def __init__(self, name, rows=None):
+        self.name = name
+        if name == 'hubbard':
+            self.paulis, self.coeffs = hubbard_jw(4, 4, 1.0, 4.0, periodic=True)
+            self.D, self.seed = 1 << 20, 1
+            self.blocks = [(16, 8), (16, 8)]
+            self.vtype = 'c64'
+            self.label = 'hubbard4x4_periodic_t1_U4_jw32_D1048576_sector8u8d'
+            self.lobpcg = True
+        elif name == 'chemistry':
+            self.paulis, self.coeffs = chemistry_jw(32, np.random.default_rng(4), keep=50000)
+            self.D, self.seed = 1 << 26, 5
+            self.blocks = [(32, 16), (32, 16)]
+            self.vtype = 'c64'
+            self.label = 'chemistry32orb_jw64_K50000_D67108864_sector16a16b'
+            self.lobpcg = False
+        elif name == 'random20':
+            self.paulis, self.coeffs = random_pauli_sum(np.random.default_rng(20), 20, 200)
+            self.D, self.seed = 16384, 20
+            self.blocks = [(20, 10)]
+            self.vtype = 'c128'
+            self.label = 'random20_K200_loc1to4_D16384_weight10'
+            self.lobpcg = True
+        else:
+            raise ValueError(f'unknown workload {name}')
+        if rows:
+            self.D = int(rows)
+            self.label += f'_rows{self.D}'
+        self.num_qubits = sum(nb for nb, _ in self.blocks)
+        self.S = sample_sector(np.random.default_rng(self.seed), self.D, self.blocks)
+        self.x = random_vector(np.random.default_rng(self.seed + 1), self.D, complex_=True)
+
+
 def random_vector(rng, D, complex_=True, dtype=np.complex128):
     """Normalised complex-normal (or real normal) vector."""
     if complex_:

@@ -15,6 +15,10 @@ def _tree_index(xs, i):
         return type(xs)(_tree_index(x, i) for x in xs)
     if isinstance(xs, dict):
         return {k: _tree_index(v, i) for k, v in xs.items()}
+    if hasattr(type(xs), '_shim_data'):  # registered dataclass: slice the data fields
+        kw = {k: _tree_index(getattr(xs, k), i) for k in type(xs)._shim_data}
+        kw.update({k: getattr(xs, k) for k in type(xs)._shim_static})
+        return type(xs)(**kw)
     return asjarray(_np.asarray(xs)[i])
 
 
@@ -23,6 +27,8 @@ def _tree_len(xs):
         return _tree_len(xs[0])
     if isinstance(xs, dict):
         return _tree_len(next(iter(xs.values())))
+    if hasattr(type(xs), '_shim_data'):
+        return _tree_len(getattr(xs, type(xs)._shim_data[0]))
     return _np.asarray(xs).shape[0]
 
 

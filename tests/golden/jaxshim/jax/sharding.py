@@ -1,6 +1,11 @@
 """``jax.sharding`` stand-in: no mesh is ever active."""
 
 
+class NamedSharding:
+    def __init__(self, mesh=None, spec=None):
+        self.mesh, self.spec = mesh, spec
+
+
 class PartitionSpec(tuple):
     def __new__(cls, *args):
         return super().__new__(cls, args)

@@ -2,13 +2,18 @@
 
 Run in a container that has the rqutils sources (read-only) but no jax:
 
-    python tests/golden/make_golden.py /path/to/rqutils-checkout
+    python tests/golden/make_golden.py /path/to/rqutils-checkout            # SQD cases
+    python tests/golden/make_golden.py /path/to/rqutils-checkout --svsim    # svsim cases
 
 The reference modules ``rqutils/paulis/symplectic.py``, ``rqutils/sqd.py`` and
 ``rqutils/ground_locg.py`` are imported unmodified; ``jax`` is provided by the NumPy stand-in in
 ``tests/golden/jaxshim`` (eager execution, 64-bit).  Package ``__init__`` files are bypassed
 (they need installed metadata and unrelated modules).  Each case writes ``case_<name>.npz`` next
 to this script with the inputs, the reference's intermediate arrays and its final outputs.
+
+With ``--svsim`` the reference's state-vector simulator ``rqutils/svsim.py`` is imported the same
+way and each circuit case writes ``svsim_<name>.npz``: the gate list, the reference's CircuitXZ
+arrays (``to_circuitxz``), the initial state and the final state of ``svsim``.
 """
 import os
 import sys
@@ -210,10 +215,72 @@ def fullspace_case(PauliSumXZ, rng):
     # symplectic.py:146, so only the 1-d form is recorded.)
 
 
+def svsim_cases():
+    """Random circuits of every gate kind the reference accepts in a gate list (x, y, z, rx, ry,
+    rz, rzz), one-hot and dense initial states, angles including 0 and +-2 pi."""
+    rng = np.random.default_rng(20261204)
+    names = ['x', 'y', 'z', 'rx', 'ry', 'rz', 'rzz']
+
+    def circuit(n, ngates, angles=None):
+        out = []
+        for _ in range(ngates):
+            nm = names[rng.integers(len(names))]
+            if nm == 'rzz':
+                q = [int(v) for v in rng.choice(n, size=2, replace=False)]
+            else:
+                q = int(rng.integers(n))
+            if nm.startswith('r'):
+                th = float(rng.uniform(-np.pi, np.pi)) if angles is None else float(rng.choice(angles))
+                out.append((nm, q, th))
+            else:
+                out.append((nm, q))
+        return out
+
+    dense8 = rng.normal(size=256) + 1j * rng.normal(size=256)
+    return {
+        'mixed6': (circuit(6, 40), 5),
+        'dense8': (circuit(8, 60), dense8 / np.linalg.norm(dense8)),
+        'edge5': (circuit(5, 30, angles=[0., 2 * np.pi, -2 * np.pi, np.pi, -np.pi / 2]) +
+                  [('rx', 4, 0.3), ('x', 4), ('rzz', [0, 4], 1.1)], 0),
+        'deep10': (circuit(10, 200), 1023),
+    }
+
+
+def run_svsim_case(rsv, circ, init):
+    names = np.array([g[0] for g in circ])
+    qubits = np.full((len(circ), 2), -1, dtype=np.int64)
+    angles = np.zeros(len(circ))
+    for k, g in enumerate(circ):
+        q = np.atleast_1d(np.asarray(g[1], dtype=np.int64))
+        qubits[k, :len(q)] = q
+        if len(g) > 2:
+            angles[k] = g[2]
+    cxz = rsv.to_circuitxz(circ)
+    init_arg = np.int64(init) if np.ndim(init) == 0 else np.asarray(init, dtype=np.complex128)
+    final = np.asarray(rsv.svsim(circ, init_arg))
+    return dict(names=names, qubits=qubits, angles=angles, x=np.asarray(cxz.x),
+                z=np.asarray(cxz.z), cos=np.asarray(cxz.cos), sin=np.asarray(cxz.sin),
+                num_qubits=np.int64(cxz.num_qubits), initial=np.asarray(init_arg), final=final)
+
+
+def main_svsim(root):
+    load_reference(root)
+    import rqutils.svsim as rsv
+    for name, (circ, init) in svsim_cases().items():
+        data = run_svsim_case(rsv, circ, init)
+        np.savez_compressed(os.path.join(HERE, f'svsim_{name}.npz'), **data)
+        print(f'svsim {name}: n={int(data["num_qubits"])} gates={len(circ)} '
+              f'|psi|={np.linalg.norm(data["final"]):.15f}')
+
+
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('RQUTILS_REFERENCE')
+    args = [a for a in sys.argv[1:] if not a.startswith('--')]
+    root = args[0] if args else os.environ.get('RQUTILS_REFERENCE')
     if not root or not os.path.isdir(os.path.join(root, 'rqutils')):
-        raise SystemExit('usage: make_golden.py <rqutils checkout>')
+        raise SystemExit('usage: make_golden.py <rqutils checkout> [--svsim]')
+    if '--svsim' in sys.argv:
+        main_svsim(root)
+        return
     rsqd, rlocg, PauliSumXZ = load_reference(root)
     rng = np.random.default_rng(7)
     for name, case in build_cases().items():

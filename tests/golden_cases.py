@@ -29,3 +29,21 @@ def packed_to_u64(packed, n, padded=True):
 
 def hamiltonian(case):
     return [str(p) for p in case['paulis']], case['coeffs']
+
+
+def svsim_case_names():
+    return sorted(os.path.basename(p)[6:-4] for p in glob.glob(os.path.join(GOLDEN, 'svsim_*.npz')))
+
+
+def load_svsim(name):
+    """A state-vector fixture recorded from the reference's rqutils/svsim.py, with its gate list
+    rebuilt as (name, qubit(s)[, angle]) specifiers."""
+    d = dict(np.load(os.path.join(GOLDEN, f'svsim_{name}.npz'), allow_pickle=False))
+    circ = []
+    for nm, q, th in zip(d['names'], d['qubits'], d['angles']):
+        nm = str(nm)
+        qq = [int(v) for v in q if v >= 0]
+        qarg = qq if nm == 'rzz' else qq[0]
+        circ.append((nm, qarg, float(th)) if nm.startswith('r') else (nm, qarg))
+    d['circuit'] = circ
+    return d

@@ -68,9 +68,9 @@ def test_host_only_entry_points(libpath):
 
 def test_struct_layouts():
     from rqutils_gb300 import _lib as L
-    assert ctypes.sizeof(L.Subspace) == 88
+    assert ctypes.sizeof(L.Subspace) == 104
     assert ctypes.sizeof(L.Terms) == 56
-    assert ctypes.sizeof(L.Operator) == 88 + 56 + 8 + 40 + 8
+    assert ctypes.sizeof(L.Operator) == 104 + 56 + 8 + 40 + 8
     assert ctypes.sizeof(L.LobpcgParams) == 64
     assert ctypes.sizeof(L.LobpcgResult) == 48
     assert ctypes.sizeof(L.Batch) == 208
@@ -96,3 +96,34 @@ def test_terms_upload_validates_on_the_host(libpath):
     bad = np.array([0, 2, 1], np.int32)          # does not end at K
     args = [xm2.ctypes.data, bad.ctypes.data, zm.ctypes.data, cf.ctypes.data] + [dummy] * 5
     assert lib.rq_terms_upload(2, 2, *args, ctypes.byref(t), None) == L.E_ARG
+
+
+def test_struct_layouts_match_the_c_header(tmp_path):
+    """The ctypes structures have the sizes and field offsets the C compiler gives the header's
+    structures (gcc on include/rqsqd.h)."""
+    import shutil
+    import subprocess
+    from rqutils_gb300 import _lib as L
+    cc = shutil.which('gcc') or shutil.which('cc')
+    if cc is None:
+        pytest.skip('no C compiler')
+    structs = {'rq_subspace_t': L.Subspace, 'rq_terms_t': L.Terms, 'rq_operator_t': L.Operator,
+               'rq_lobpcg_params_t': L.LobpcgParams, 'rq_lobpcg_result_t': L.LobpcgResult,
+               'rq_batch_t': L.Batch}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rqsqd.h"', 'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'printf("{cname}.{f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / 'layout.c'
+    src.write_text('\n'.join(lines))
+    exe = tmp_path / 'layout'
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 'include')
+    subprocess.run([cc, '-I', inc, str(src), '-o', str(exe)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                    text=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert int(got[f'{cname}.{f[0]}']) == getattr(py, f[0]).offset, (cname, f[0])

@@ -313,12 +313,14 @@ def test_persistent_loop_matches_graph_loop(cache_level, variant):
         assert abs(torch.vdot(x1, x2).item()) > 1 - 1e-10
 
 
+@pytest.mark.parametrize('tags', [True, False])
 @pytest.mark.parametrize('key_bits', [32, 64])
 @pytest.mark.parametrize('sectors', ['one', 'two', 'off'])
-def test_hash_kernel_sector_filter_modes(sectors, key_bits):
+def test_hash_kernel_sector_filter_modes(sectors, key_bits, tags):
     """The FREE hash kernel's three filter forms -- a subspace in one (popcount a, popcount b)
     sector (two popcount compares), several sectors (the bitset) and the filter off -- give the
-    oracle's product, and all three agree bit for bit with each other."""
+    oracle's product, and all three agree bit for bit with each other, probing the tag words or
+    the key buckets."""
     import torch
     from oracle import sqd as osqd
     from oracle.paulis import from_paulisum as oterms
@@ -338,13 +340,80 @@ def test_hash_kernel_sector_filter_modes(sectors, key_bits):
     v = workloads.random_vector(rng, len(S))
     ref = osqd.matvec_xcached(v, osqd.xsources_all(S, ot), ot, S)
     fm = (0, 0) if sectors == 'off' else None
-    sub = DeviceSubspace(S, num_qubits=n, filter_masks=fm, key_bits=key_bits)
+    sub = DeviceSubspace(S, num_qubits=n, filter_masks=fm, key_bits=key_bits, tags=tags)
     bits = int(np.bitwise_count(sub.fbits.cpu().numpy().view(np.uint32)).sum())
     assert bits == {'one': 1, 'two': 2, 'off': bits}[sectors]
+    assert (sub.c.fpoint >= 0) == (sectors == 'one')
     op = DeviceOperator(DeviceTerms(h), sub, mode='free')
     y = op.matvec(torch.as_tensor(v).cuda()).cpu().numpy()
     op.check_errors()
     assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref)
-    other = DeviceSubspace(S, num_qubits=n, filter_masks=(0, 0), key_bits=key_bits)
+    other = DeviceSubspace(S, num_qubits=n, filter_masks=(0, 0), key_bits=key_bits,
+                           tags=not tags)
     y0 = DeviceOperator(DeviceTerms(h), other, mode='free').matvec(torch.as_tensor(v).cuda()).cpu().numpy()
     np.testing.assert_array_equal(y, y0)
+
+
+@pytest.mark.parametrize('key_bits', [32, 64])
+@pytest.mark.parametrize('dtype', ['float32', 'float64', 'complex64', 'complex128'])
+def test_tag_words_match_key_buckets(key_bits, dtype):
+    """2^16 states (buckets with three or four keys and keys moved on from full buckets occur):
+    the matrix-free product through the tag words equals, bit for bit, the product through the
+    key buckets and the cached-connectivity product."""
+    import torch
+    from rqutils_gb300 import workloads
+    from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    rng = np.random.default_rng(505)
+    n = 24
+    labels, coeffs = workloads.random_pauli_sum(rng, n, 400)
+    S = workloads.sample_sector(rng, 1 << 16, [(12, 6), (12, 6)])
+    h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
+    terms = DeviceTerms(h)
+    with_tags = DeviceSubspace(S, num_qubits=n, key_bits=key_bits)
+    words = with_tags.htags.cpu().numpy().view(np.uint32)
+    assert (words & 0x20000000).any()                          # a bucket with three keys or more
+    halves = np.concatenate([words & 0xFFFF, words >> 16])
+    assert ((halves & 0xC000) == 0x4000).any()                 # a key moved on from a full bucket
+    no_tags = DeviceSubspace(S, num_qubits=n, key_bits=key_bits, tags=False)
+    dt = getattr(torch, dtype)
+    if not dt.is_complex and not terms.is_real:
+        pytest.skip('complex coefficients need complex vectors')
+    x = torch.as_tensor(rng.normal(size=len(S)) + 1j * rng.normal(size=len(S)))
+    x = (x if dt.is_complex else x.real).to(dt).cuda()
+    a = DeviceOperator(terms, with_tags, mode='free')
+    y = a.matvec(x)
+    a.check_errors()
+    assert torch.equal(y, DeviceOperator(terms, no_tags, mode='free').matvec(x))
+    assert torch.equal(y, DeviceOperator(terms, with_tags, mode='conn').matvec(x))
+
+
+@pytest.mark.parametrize('tags', [True, False])
+def test_hash_kernel_streams_more_than_16384_groups(tags):
+    """A Pauli sum with more X groups than shared memory holds (the group keys are streamed in
+    tiles): the matrix-free product equals the oracle's row-by-row product and, bit for bit, the
+    cached-connectivity product."""
+    import torch
+    from oracle import sqd as osqd
+    from oracle.paulis import from_paulisum as oterms
+    from rqutils_gb300 import workloads
+    from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    rng = np.random.default_rng(606)
+    n = 22
+    labels, coeffs = workloads.random_pauli_masks(rng, n, 60000, locality=(3, 8))
+    S = workloads.sample_sector(rng, 3000, [(11, 5), (11, 6)])
+    h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
+    assert len(h.xmask) > 20000
+    ot = oterms((labels, coeffs), force_real=True)
+    v = workloads.random_vector(rng, len(S))
+    ref, hits = osqd.rows_matvec(v, ot, S, np.arange(len(S)))
+    assert sum(len(r) for r in hits) > 1000
+    terms = DeviceTerms(h)
+    sub = DeviceSubspace(S, num_qubits=n, tags=tags)
+    free = DeviceOperator(terms, sub, mode='free')
+    y = free.matvec(torch.as_tensor(v).cuda())
+    free.check_errors()
+    yh = y.cpu().numpy()
+    assert np.linalg.norm(yh - ref) <= 1e-12 * np.linalg.norm(ref)
+    assert torch.equal(y, DeviceOperator(terms, sub, mode='conn').matvec(torch.as_tensor(v).cuda()))

@@ -81,3 +81,15 @@ def test_reference_errors():
         svsim([('cz', [0, 1])])
     with pytest.raises(ValueError):
         svsim([('h', 0)])
+
+
+@pytest.mark.parametrize('name', __import__('golden_cases').svsim_case_names())
+def test_svsim_matches_reference_fixtures(name):
+    """rq_svsim against final states recorded from the unmodified reference rqutils/svsim.py:
+    bit for bit (values compared with ==, so only the sign of a zero may differ)."""
+    from golden_cases import load_svsim
+    from rqutils_gb300.svsim import svsim
+    d = load_svsim(name)
+    init = d['initial'] if d['initial'].ndim else int(d['initial'])
+    got = svsim(d['circuit'], init)
+    np.testing.assert_array_equal(got.cpu().numpy(), d['final'])

@@ -53,3 +53,21 @@ def test_circuit_conversion_matches_oracle():
     assert to_circuitxz(a) is a and isinstance(a, CircuitXZ)
     with pytest.raises(ValueError):
         to_circuitxz([('cz', [0, 1])])
+
+
+@pytest.mark.parametrize('name', __import__('golden_cases').svsim_case_names())
+def test_oracle_matches_reference_svsim_fixtures(name):
+    """The oracle restatement against outputs of the unmodified reference rqutils/svsim.py
+    (recorded through the NumPy stand-in for jax): circuit arrays and final states bit for bit."""
+    from golden_cases import load_svsim
+    from rqutils_gb300.svsim import to_circuitxz
+    d = load_svsim(name)
+    x, z, c, s, n = osv.to_circuitxz(d['circuit'])
+    for got, want in ((x, d['x']), (z, d['z']), (c, d['cos']), (s, d['sin'])):
+        np.testing.assert_array_equal(got, want)
+    assert n == int(d['num_qubits'])
+    cx = to_circuitxz(d['circuit'])
+    for got, want in ((cx.x, d['x']), (cx.z, d['z']), (cx.cos, d['cos']), (cx.sin, d['sin'])):
+        np.testing.assert_array_equal(got, want)
+    init = d['initial'] if d['initial'].ndim else int(d['initial'])
+    np.testing.assert_array_equal(osv.svsim(x, z, c, s, n, init), d['final'])

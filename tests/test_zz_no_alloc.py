@@ -1,9 +1,10 @@
 """rq_lobpcg_solve_noalloc: the solve for callers that cannot allocate device memory.
 
-Such callers (a framework that owns the allocator, work recorded into a CUDA graph, memory
-reserved up front) pass only their inputs and outputs; the solver's workspace is a static device
-array of the library.  This file is collected last so that a run stopping at the first failure
-has already run every other test; it also passes on its own in a fresh process.
+Such callers -- a custom-call handler inside another framework, handed only its operand and result
+buffers, or a service that reserved its device memory at start-up -- pass only their inputs and
+outputs; the solver's workspace is a static device array of the library.  This file is collected
+last so that a run stopping at the first failure has already run every other test; it also passes
+on its own in a fresh process.
 """
 import ctypes
 import warnings
@@ -92,3 +93,27 @@ def test_noalloc_rejects_oversized_problem():
                                          ctypes.byref(res), None)
     assert rc == L.E_RANGE
     assert b'static workspace holds' in L.lib().rq_last_error()
+
+
+def test_noalloc_leaves_device_free_memory_unchanged():
+    """The call allocates nothing: once a first call on the device has loaded the solver's kernels
+    and looked up the static array's address, a further call leaves the device's free memory
+    (cudaMemGetInfo) exactly as it was."""
+    import torch
+    from rqutils_gb300 import _lib as L
+    prob = _operator('hubbard2x2')
+    x0 = prob.initial_vector()
+    vt = L.F64 if prob.terms.is_real else L.C128
+    prm = L.LobpcgParams(maxiter=1000, variant=L.LOBPCG_REFERENCE, vtype=vt, use_graph=1)
+    first, _ = _solve_noalloc(prob.op, x0, prm)
+    xo = torch.empty_like(x0)
+    res = L.LobpcgResult()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    rc = L.lib().rq_lobpcg_solve_noalloc(ctypes.byref(prob.op.c), ctypes.byref(prm), L.ptr(x0),
+                                         L.ptr(xo), ctypes.byref(res), L.stream_ptr())
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert rc == L.OK and res.converged
+    assert res.eigval == first.eigval
+    assert free_after == free_before, free_before - free_after
