@@ -85,14 +85,17 @@ typedef struct rq_subspace {
     uint32_t *pmap;          /* [2^pbits / 32]: bit (hash(s) >> (32 - pbits)) set for every
                                 state, written by rq_subspace_build; a lookup whose bit is
                                 clear skips the table (NULL = none)                        */
-    uint32_t *htags;         /* [1 << hbits] (4 bytes per bucket) or NULL, written by
-                                rq_subspace_build: 16-bit tags of the bucket's first two key
-                                slots (0 = empty, else 0x8000 for a key in its home bucket or
-                                0x4000 for a key moved on from a full bucket, | the low 13
-                                bits of the key's 32-bit hash), bit 13 of the upper tag set
-                                when slot 2 is occupied too.  The matrix-free kernel probes
-                                these words instead of the key buckets and reads the keys only
-                                where a tag matches or the bucket holds more keys           */
+    uint32_t *lmap;          /* line filter, [2^lbits lines of 2^lwbits bits] or NULL: bit
+                                (hash(s) mod 2^lwbits) of line (hash(s >> lshift) >> (32 -
+                                lbits)) set for every state, written by rq_subspace_build.
+                                States that agree above bit lshift share a line, and so do
+                                their targets under one X mask: the rows of a warp (consecutive
+                                sorted states) probe a few lines instead of one line per lane.
+                                A clear bit is a miss; a set bit is resolved in the table    */
+    int32_t   lbits;         /* log2(lines) of lmap, from rq_line_filter_bits               */
+    int32_t   lwbits;        /* log2(bits per line): 8 (32-byte lines) .. 10 (128-byte)     */
+    int32_t   lshift;        /* written by rq_subspace_build: the prefix shift, chosen so that
+                                about 2^(lwbits - 5) states share a prefix on average        */
     int32_t   fpoint;        /* written by rq_subspace_build: pa * 65 + pb when every state has
                                 the same pair pa = popcount(s & fmask_a), pb = popcount(s &
                                 fmask_b) (a subspace in one sector), else -1; -1 with the
@@ -135,6 +138,10 @@ int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits);
  * (<= 64 MB), else pbits = min(29, hbits + 2) (at most 64 MB of bitmap, a bit set for ~1/8 of
  * the misses).  The bitmap takes 2^pbits / 8 bytes. */
 int rq_presence_bits(int64_t D, int32_t key_bits, int32_t *pbits);
+
+/* Line-filter size for D states and 2^lwbits bits per line (lwbits 8..10): 2^lbits lines, each
+ * holding 2^(lwbits - 7) states on average; the filter takes 2^(lbits + lwbits - 3) bytes. */
+int rq_line_filter_bits(int64_t D, int32_t lwbits, int32_t *lbits);
 
 /* Bytes of scratch that rq_matvec / rq_conn_build / rq_dots need for their reductions/scans. */
 int rq_scratch_size(int64_t D, size_t *bytes);

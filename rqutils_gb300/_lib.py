@@ -27,7 +27,8 @@ class Subspace(ctypes.Structure):
                 ('key_bits', ctypes.c_int32), ('pbits', ctypes.c_int32),
                 ('empty_key', ctypes.c_uint64), ('fmask_a', ctypes.c_uint64),
                 ('fmask_b', ctypes.c_uint64), ('fbits', _c_void_p), ('pmap', _c_void_p),
-                ('htags', _c_void_p), ('fpoint', ctypes.c_int32)]
+                ('lmap', _c_void_p), ('lbits', ctypes.c_int32), ('lwbits', ctypes.c_int32),
+                ('lshift', ctypes.c_int32), ('fpoint', ctypes.c_int32)]
 
 
 class Terms(ctypes.Structure):
@@ -99,6 +100,7 @@ SIGNATURES = {
                                        _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
                                        _c_void_p, _c_void_p, _P(Terms), _c_void_p]),
     'rq_terms_hash': (ctypes.c_int, [_P(Terms), _c_void_p, _c_void_p]),
+    'rq_line_filter_bits': (ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int32)]),
     'rq_terms_group_scratch_size': (ctypes.c_int, [ctypes.c_int64, _P(ctypes.c_size_t)]),
     'rq_terms_group': (ctypes.c_int, [ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
                                       ctypes.c_int32, _c_void_p, _c_void_p, _c_void_p, _c_void_p,

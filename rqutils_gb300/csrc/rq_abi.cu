@@ -1,4 +1,5 @@
 // Host helpers of the C ABI: error state, device properties, scratch sizing, version.
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <string>
@@ -24,16 +25,17 @@ int cuda_fail(cudaError_t e, const char *what) {
 }
 
 int sm_count() {
-    static int cached[64] = {0};
+    // per device; atomic so that threads querying at once do not race on the entry
+    static std::atomic<int> cached[64];
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-    if (cached[dev] == 0) {
-        int n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    int n = cached[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
         if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
-            n = 148;
-        cached[dev] = n;
+            n = 152;
+        cached[dev].store(n, std::memory_order_relaxed);
     }
-    return cached[dev];
+    return n;
 }
 
 size_t scratch_scan_offset() { return kScratchReduce + reduce_scratch_bytes(); }

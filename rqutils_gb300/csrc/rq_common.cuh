@@ -202,32 +202,14 @@ struct KeyWidth<32> {
     }
 };
 
-// Tag words (rq_subspace_t.htags), one 32-bit word per bucket: the 16-bit tags of slots 0 (low
-// half) and 1 (high half), 0 for an empty slot; bit 29 (bit 13 of slot 1's tag) is set when slot 2
-// is occupied as well.  Half a key per bucket on average: 1.4 % of buckets hold three or more.
-constexpr uint32_t kTagHome = 0x8000u;   // key stored in its home bucket
-constexpr uint32_t kTagMoved = 0x4000u;  // key moved on from a full bucket
-constexpr uint32_t kTagMask = 0x1FFFu;   // low bits of the key's hash
-constexpr uint32_t kTagMore = 0x20000000u;
-
-// One bucket's tag word in a single 32-bit read-only load; 0 (no tags) when pred is false.
-__device__ __forceinline__ uint32_t load_tags(const uint32_t *p, bool pred) {
+// One 32-bit word of the line filter in a single read-only load; 0 (a miss) when pred is false.
+__device__ __forceinline__ uint32_t load_word(const uint32_t *p, bool pred) {
     uint32_t w = 0u;
     asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t"
         "@q ld.global.nc.u32 %0, [%1];\n\t}"
         : "+r"(w)
         : "l"(p), "r"((unsigned)pred));
     return w;
-}
-
-// Tag test of target hash h against a tag word: hot when slot 0 or 1 holds a home-bucket key with
-// h's tag (a zero 16-bit lane of the word ^ tag, found with the borrow test (v - 1) & ~v & 0x8000
-// per lane, which is exact for "some lane is zero") or when the bucket holds more keys than the
-// word shows.  The word 0 (no keys, or a probe that was skipped) is never hot.
-__device__ __forceinline__ bool tags_hot(uint32_t w, uint32_t h) {
-    const uint32_t rep = (kTagHome | (h & kTagMask)) * 0x00010001u;
-    const uint32_t v = (w & ~kTagMore) ^ rep;
-    return (((v - 0x00010001u) & ~v & 0x80008000u) | (w & kTagMore)) != 0u;
 }
 
 // Branch-free bucket test: `any` when a slot equals t, `open` when the last slot is empty.
@@ -269,12 +251,14 @@ static __device__ __noinline__ int probe_rest(const rq_subspace_t &S, uint64_t t
 }
 
 // Full lookup of t starting at bucket b.  The empty key is not a state, so a target equal to it
-// is a miss (it would otherwise match an empty slot, whose row index is undefined).
+// is a miss (it would otherwise match an empty slot, whose row index is undefined).  With 32-bit
+// keys every state is below 2^32, so a target at or above it (an X mask with high bits) is a miss
+// too: its low 32 bits alone could equal a stored key.
 template <int KB>
 __device__ __forceinline__ int lookup_hash_at(const rq_subspace_t &S, uint64_t t, uint32_t b,
                                               int *err) {
     using K = typename KeyWidth<KB>::K;
-    if (t == S.empty_key) return -1;
+    if (t == S.empty_key || (KB == 32 && (t >> 32) != 0)) return -1;
     const auto bk = KeyWidth<KB>::load(bucket_ptr<KB>(S, b), true, S.empty_key);
     const int s = slot_of(bk, (K)t);
     if (s >= 0) return S.hvals[(size_t)b * kBucketSlots + s];

@@ -59,4 +59,44 @@ inline int64_t *scratch_scan(void *scratch) {
 
 int vtype_size(int32_t vtype);
 
+// Launch settings of one kernel: the dynamic shared memory it has been opted into and its
+// occupancy at one shared-memory size.  Each launcher keeps one entry per host thread and device
+// (cache_slot), so threads never share an entry and devices with different SM counts or
+// attributes never see each other's values.
+struct KernelLaunchCache {
+    size_t configured = 0;
+    size_t occ_smem = ~size_t(0);
+    int occ_blocks = 1;
+};
+constexpr int kMaxCachedDevices = 64;
+
+// Opt kern into smem bytes of dynamic shared memory (above the 48 KB default) and return its
+// resident blocks per SM at `block` threads, querying the runtime only when `c` does not hold the
+// answer yet (the occupancy query is also reached while a stream is being captured, where only
+// stream work should be issued).
+template <typename KernT>
+int configure_kernel(KernT kern, KernelLaunchCache &c, size_t smem, int block, int *per_sm) {
+    if (smem > 48 * 1024 && smem > c.configured) {
+        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        c.configured = smem;
+    }
+    if (c.occ_smem != smem) {
+        int per = 0;
+        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, block, smem));
+        c.occ_blocks = per < 1 ? 1 : per;
+        c.occ_smem = smem;
+    }
+    *per_sm = c.occ_blocks;
+    return RQ_OK;
+}
+
+// This thread's entry for the current device in a launcher's table.
+inline int cache_slot(KernelLaunchCache (&table)[kMaxCachedDevices], KernelLaunchCache **out) {
+    int dev = 0;
+    RQ_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxCachedDevices) return fail(RQ_E_RANGE, "device index out of range");
+    *out = &table[dev];
+    return RQ_OK;
+}
+
 }  // namespace rq

@@ -365,7 +365,10 @@ k_mask(SEG seg, const V *v, V *p) {
 // FAST projection in one pass, no reduction: p = m (v - d0 x - d1 y) with d0, d1 from
 // red[kIp0], red[kIp1] and w = |v - d0 x - d1 y|^2 in red[kVn] (all three from the six inner
 // products, d_proj_coef); m = 1 / sqrt(w), or 0 when w < thr^2 |v|^2 (v numerically inside the
-// span of x, y; the role of the 0.99 cut of ground_locg.py:421), |v|^2 in red[kG10 + 5].
+// span of x, y; the role of the 0.99 cut of ground_locg.py:421), |v|^2 in red[kG10 + 5].  w comes
+// from a difference of inner products, whose rounding floor is about eps |v|^2; the FP64 cut
+// thr = 1e-7 (thr^2 = 1e-14) stays above that floor, so a w that is only rounding is never used
+// to scale p (a wrong scale would make the Rayleigh-Ritz basis non-orthonormal).
 template <typename V, typename SEG>
 __device__ __forceinline__ void d_sub2_scale(SEG seg, const V *x, const V *y, const V *v, V *p) {
     State *st = seg.state();
@@ -374,7 +377,7 @@ __device__ __forceinline__ void d_sub2_scale(SEG seg, const V *x, const V *y, co
     BLOCK_R(5, {
         const double n2 = st->red[kVn].x;
         const double r2 = st->red[kG10 + 5].x;
-        const double thr = sizeof(R) == 4 ? 1e-5 : 1e-10;
+        const double thr = sizeof(R) == 4 ? 1e-5 : 1e-7;
         const double m = (n2 > 0. && n2 > thr * thr * r2) ? 1. / sqrt(n2) : 0.;
         out[0] = (R)m;
         out[1] = (R)(-m * st->red[kIp0].x);

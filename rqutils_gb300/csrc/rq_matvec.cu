@@ -158,19 +158,33 @@ __device__ inline void load_lookup_smem(const rq_subspace_t &S, uint32_t *fb, ui
 // a group are read from global memory only on a hit.  U bucket loads are issued together; the
 // loop only marks "hot" groups (a key match, a full bucket, or a target equal to the empty key)
 // in a 64-bit mask, resolved once per 64 groups so that the rare divergent work is not
-// interleaved with the probes.  The limit at D = 2^20 (tables in L2) is the L1 data pipe: each
-// bucket load is one 16- or 32-byte read at a random address, one wavefront per lane.
+// interleaved with the probes.  Each bucket load is one 16- or 32-byte read at a random address,
+// one L1 wavefront per lane; at D = 2^20 (tables in L2) those wavefronts are the limit.
+//
+// With the line filter (rq_subspace_t.lmap) the probe is a bit test in a line chosen by the
+// target's prefix t >> lshift: the rows of a warp are consecutive sorted states that share their
+// high bits, so for one X group their targets share them too and the warp's probes fall in a few
+// lines (one wavefront each) instead of one line per lane.  Set bits are resolved in the table.
 
 // Group keys live in shared memory for the whole launch: (x_j, h(x_j)) packed as uint2 for 32-bit
-// keys (8 B per group) or as uint64 + uint32 arrays for 64-bit keys (12 B per group).  The x = 0
-// group is left out of the list (its diagonal is applied before the probes), so that the probe
-// loop has no per-group skip test; resident index c is group c + (c >= diag_group).  Large J
-// runs one 1024-thread block per SM so that up to kMaxResidentGroups fit.
-constexpr int kMaxResidentGroups = 16384;
+// keys or as uint64 + uint32 arrays for 64-bit keys, then the line hash hl_j = h(x_j >> lshift)
+// (12 or 16 B per group).  The x = 0 group is left out of the list (its diagonal is applied before
+// the probes), so that the probe loop has no per-group skip test; resident index c is group
+// c + (c >= diag_group).  Large J runs one 1024-thread block per SM so that up to
+// max_resident_groups fit; above that the keys are streamed through in tiles.
+template <int KB>
+__host__ __device__ constexpr int max_resident_groups() {
+    return KB == 32 ? 16384 : 12288;  // 192 KB of shared memory either way
+}
 
 template <int KB>
 __host__ __device__ inline size_t group_key_bytes(int J) {
-    return KB == 32 ? (size_t)J * 8 : align16((size_t)J * 8) + (size_t)J * 4;
+    return align16((size_t)J * 8) + (KB == 32 ? 0 : align16((size_t)J * 4)) + (size_t)J * 4;
+}
+
+template <int KB>
+__host__ __device__ inline size_t group_line_offset(int kt) {
+    return align16((size_t)kt * 8) + (KB == 32 ? 0 : align16((size_t)kt * 4));
 }
 
 // Sector filter of the hash kernel: none, the general (popcount a, popcount b) bitset, or the
@@ -184,12 +198,15 @@ __shared__ uint32_t hk_htab[kHashTableWords];
 extern __shared__ __align__(16) unsigned char hk_dyn[];
 
 // Group keys of resident indices [c0, c0 + cn) into shared-memory slots [0, cn); the layout holds
-// kt slots (32-bit keys: (x, h(x)) pairs; 64-bit keys: x masks, then hashes).  Resident index c is
-// group c + (c >= diag_group).  All threads of the block call it.
+// kt slots (32-bit keys: (x, h(x)) pairs; 64-bit keys: x masks, then hashes; then the line hashes
+// h(x >> lshift)).  Resident index c is group c + (c >= diag_group).  All threads of the block
+// call it.
 template <int KB>
-__device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int cn, int kt) {
+__device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int cn, int kt,
+                                                int lshift) {
     constexpr int NB = KeyWidth<KB>::kNbytes;
     const int skip = T.diag_group;
+    uint32_t *hl = reinterpret_cast<uint32_t *>(hk_dyn + group_line_offset<KB>(kt));
     for (int c = threadIdx.x; c < cn; c += blockDim.x) {
         const int j = c0 + c + (skip >= 0 && c0 + c >= skip);
         const uint64_t xv = T.xmask[j];
@@ -200,52 +217,60 @@ __device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int
             reinterpret_cast<uint64_t *>(hk_dyn)[c] = xv;
             reinterpret_cast<uint32_t *>(hk_dyn + align16((size_t)kt * 8))[c] = h;
         }
+        hl[c] = lin_hash(hk_htab, lshift < 64 ? xv >> lshift : 0ULL, NB);
     }
 }
 
 // Probes in flight per thread: four with key buckets (a 16- or 32-byte bucket per probe fills the
-// 40 registers of six resident 256-thread blocks), eight with tag words (one register per probe)
-// where that fits the registers without spills (ptxas -v): 32-bit keys without the bitset
+// 40 registers of six resident 256-thread blocks), eight with the line filter (one word per
+// probe) where that fits the registers without spills (ptxas -v): 32-bit keys without the bitset
 // filter.  A divisor of the 64 groups of a super-chunk.
-#ifndef RQ_TAG_PROBES
-#define RQ_TAG_PROBES 8
+#ifndef RQ_LINE_PROBES
+#define RQ_LINE_PROBES 8
 #endif
 constexpr int kKeyProbes = 4;
 
 template <typename V, int KB, int FM>
-constexpr int tag_probes() {
-    return (FM == kFiltSet || KB == 64) ? 4 : RQ_TAG_PROBES;
+constexpr int line_probes() {
+    return (FM == kFiltSet || KB == 64) ? 4 : RQ_LINE_PROBES;
 }
 
-// TL: the group keys may need streaming in tiles (1024-thread kernels only; with 256-thread blocks
-// they always fit and the tile loop is one pass known at compile time).
-template <typename V, int KB, int FM, bool TG, bool TL>
+// LF: probe the line filter.  TL: the group keys may need streaming in tiles (1024-thread kernels
+// only; with 256-thread blocks they always fit and the tile loop is one pass known at compile
+// time).
+template <typename V, int KB, int FM, bool LF, bool TL>
 __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__restrict__ x,
                                           V *__restrict__ y, int *err, int pa0, int pb0) {
     using R = typename VT<V>::R;
     using K = typename KeyWidth<KB>::K;
     constexpr int NB = KeyWidth<KB>::kNbytes;
     constexpr int kBucketBytes = KeyWidth<KB>::kBucketBytes;
-    constexpr int U = TG ? tag_probes<V, KB, FM>() : kKeyProbes;
+    constexpr int U = LF ? line_probes<V, KB, FM>() : kKeyProbes;
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
     const int64_t D = S.D;
     const int skip = T.diag_group;  // the x = 0 group is applied outside the probe loop
     const int nres = T.J - (skip >= 0 ? 1 : 0);  // groups of the probe loop
     // shared-memory slots: every group's keys when they fit (loaded once by the kernel), else
-    // tiles of kMaxResidentGroups streamed through for every row batch
-    const int kt = (!TL || nres <= kMaxResidentGroups) ? nres : kMaxResidentGroups;
+    // tiles of max_resident_groups streamed through for every row batch
+    constexpr int kMaxRes = max_resident_groups<KB>();
+    const int kt = (!TL || nres <= kMaxRes) ? nres : kMaxRes;
     const bool tiled = TL && nres > kt;
     const uint2 *gk32 = reinterpret_cast<const uint2 *>(hk_dyn);
     const uint64_t *gx64 = reinterpret_cast<const uint64_t *>(hk_dyn);
     const uint32_t *gh64 = reinterpret_cast<const uint32_t *>(hk_dyn + align16((size_t)kt * 8));
+    const uint32_t *ghl = reinterpret_cast<const uint32_t *>(hk_dyn + group_line_offset<KB>(kt));
     const bool d0 = (op.diag0 != nullptr) && (skip >= 0);
     const K fa = (K)S.fmask_a, fbm = (K)S.fmask_b, empty = (K)S.empty_key;
     const int shift = 32 - S.hbits;
-    const uint32_t *pmap = S.pbits > 0 ? S.pmap : nullptr;
+    // the line filter replaces the presence bitmap
+    const uint32_t *pmap = (!LF && S.pbits > 0) ? S.pmap : nullptr;
     const int pshift = 32 - S.pbits;
     const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
-    const uint32_t *tags = S.htags;
+    const uint32_t *lmap = S.lmap;
+    const int lsh = 32 - S.lbits;                    // line = (h(s >> lshift) ^ hl_j) >> lsh
+    const int lwsh = S.lwbits - 5;                   // words per line, log2
+    const uint32_t lbmask = (1u << S.lwbits) - 1u;  // bit within the line: h(t) & lbmask
     auto sector = [&](K t) -> bool {
         if (FM == kFiltPoint) {
             int pa, pb;
@@ -273,6 +298,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
         const uint64_t s64 = __ldg(S.states + ir);
         const K s = (K)s64;
         const uint32_t hs = lin_hash(hk_htab, s64, NB);
+        const uint32_t hls = LF ? lin_hash(hk_htab, S.lshift < 64 ? s64 >> S.lshift : 0ULL, NB) : 0u;
         CAcc<R> acc;
         const cx<R> xi = VT<V>::ld(x, ir);
         if (d0) {
@@ -285,7 +311,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
             const int tn = TL ? min(kt, nres - t0) : nres;
             if (tiled) {
                 __syncthreads();  // the previous tile is no longer read
-                load_group_keys<KB>(T, t0, tn, kt);
+                load_group_keys<KB>(T, t0, tn, kt, S.lshift);
                 __syncthreads();
             }
             for (int gs0 = 0; gs0 < tn; gs0 += 64) {
@@ -294,7 +320,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
                 int g = gs0;
                 for (; g + U <= gs1; g += U) {
                     K t[U];
-                    uint32_t b[U];
+                    uint32_t b[U], ln[U];
                     bool q[U];
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
@@ -309,6 +335,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
                         }
                         q[u] = sector(t[u]);
                         b[u] = hs ^ hxg;
+                        if (LF) ln[u] = (hls ^ ghl[g + u]) >> lsh;
                     }
                     if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
                         uint32_t pw[U];
@@ -321,17 +348,19 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
                         for (int u = 0; u < U; ++u) q[u] = q[u] && ((pw[u] >> ((b[u] >> pshift) & 31)) & 1u);
                     }
                     uint32_t hb = 0u;  // hot bits of this batch, constant shifts
-                    if (TG) {
-                        // tag words: a hot lane has a home-bucket tag equal to its target's or a
-                        // bucket with more keys than the word shows (the resolution below compares
-                        // the keys).  A lane whose target fails the filter reads no word: the zero
-                        // word it keeps is never hot, so q need not stay live across the loads.
+                    if (LF) {
+                        // line filter: a hot lane's bit is set (a state, or another state's bit;
+                        // the resolution below compares the keys).  A lane whose target fails
+                        // the sector filter reads no word: the zero word it keeps is never hot,
+                        // so q need not stay live across the loads.
                         uint32_t w[U];
 #pragma unroll
-                        for (int u = 0; u < U; ++u) w[u] = load_tags(tags + (b[u] >> shift), q[u]);
+                        for (int u = 0; u < U; ++u)
+                            w[u] = load_word(lmap + ((size_t)ln[u] << lwsh) + ((b[u] & lbmask) >> 5),
+                                             q[u]);
 #pragma unroll
                         for (int u = 0; u < U; ++u)
-                            if (tags_hot(w[u], b[u])) hb |= 1u << u;
+                            if ((w[u] >> (b[u] & 31u)) & 1u) hb |= 1u << u;
                     } else {
                         typename KeyWidth<KB>::Bucket w[U];
 #pragma unroll
@@ -370,7 +399,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
 
 // FM: the sector filter's form, chosen on the host from rq_subspace_t.fpoint (one kernel per
 // form, so that the registers of the general bitset test do not weigh on the one-sector kernel)
-template <typename V, int KB, int FM, int BLOCK, bool TG>
+template <typename V, int KB, int FM, int BLOCK, bool LF>
 __global__ void __launch_bounds__(BLOCK, BLOCK == 1024 ? 1 : (sizeof(V) <= 8 ? 6 : 4))
 k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y, int *err,
               const int *gate, const int *gate2) {
@@ -383,12 +412,13 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
         for (int w = threadIdx.x; w < RQ_FILTER_WORDS; w += blockDim.x) hk_fb[w] = S.fbits[w];
     __syncthreads();
     const int nres = T.J - (T.diag_group >= 0 ? 1 : 0);
-    if (nres <= kMaxResidentGroups) load_group_keys<KB>(T, 0, nres, nres);  // else in tiles
+    if (nres <= max_resident_groups<KB>())  // else in tiles
+        load_group_keys<KB>(T, 0, nres, nres, S.lshift);
     __syncthreads();
     if (FM == kFiltPoint)
-        hash_rows<V, KB, FM, TG, BLOCK == 1024>(op, x, y, err, S.fpoint / 65, S.fpoint % 65);
+        hash_rows<V, KB, FM, LF, BLOCK == 1024>(op, x, y, err, S.fpoint / 65, S.fpoint % 65);
     else
-        hash_rows<V, KB, FM, TG, BLOCK == 1024>(op, x, y, err, 0, 0);
+        hash_rows<V, KB, FM, LF, BLOCK == 1024>(op, x, y, err, 0, 0);
 }
 
 // xhash[j] = h(xmask[j])
@@ -644,49 +674,20 @@ int launch_csr(const rq_operator_t &op, const void *x, void *y, cudaStream_t st,
 // ------------------------------------------------------------------------------------------
 // host dispatch
 // ------------------------------------------------------------------------------------------
-// Dynamic shared memory, opt-in above 48 KB and cached occupancy for one kernel instantiation.
-// The occupancy query is cached per instantiation and size (it is also reached while a stream is
-// being captured, where only stream work should be issued).
-template <typename KernT>
-int prepare_launch(KernT kern, size_t smem, size_t &configured, size_t &occ_smem, int &occ_blocks,
-                   int64_t D, int &grid) {
-    if (smem > 48 * 1024 && smem > configured) {
-        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
-    if (occ_smem != smem) {
-        int per = 0;
-        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, smem));
-        occ_blocks = per < 1 ? 1 : per;
-        occ_smem = smem;
-    }
-    int64_t g = (D + kThreads - 1) / kThreads;
-    const int64_t cap = (int64_t)sm_count() * occ_blocks;
-    if (g > cap) g = cap;
-    grid = (int)(g < 1 ? 1 : g);
-    return RQ_OK;
-}
-
-template <typename V, int KB, int FM, int BLOCK, bool TG>
+template <typename V, int KB, int FM, int BLOCK, bool LF>
 int launch_hash_block(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
                       const int *gate, const int *gate2) {
-    auto kern = k_matvec_hash<V, KB, FM, BLOCK, TG>;
+    auto kern = k_matvec_hash<V, KB, FM, BLOCK, LF>;
     const int nres = op.terms.J - (op.terms.diag_group >= 0 ? 1 : 0);
-    const size_t smem = group_key_bytes<KB>(nres < kMaxResidentGroups ? nres : kMaxResidentGroups);
-    static size_t configured = 0, occ_smem = ~size_t(0);
-    static int occ_blocks = 1;
-    if (smem > 48 * 1024 && smem > configured) {
-        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
-    if (occ_smem != smem) {
-        int per = 0;
-        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, BLOCK, smem));
-        occ_blocks = per < 1 ? 1 : per;
-        occ_smem = smem;
-    }
+    constexpr int kMaxRes = max_resident_groups<KB>();
+    const size_t smem = group_key_bytes<KB>(nres < kMaxRes ? nres : kMaxRes);
+    thread_local KernelLaunchCache table[kMaxCachedDevices];
+    KernelLaunchCache *c = nullptr;
+    int per_sm = 1;
+    RQ_TRY(cache_slot(table, &c));
+    RQ_TRY(configure_kernel(kern, *c, smem, BLOCK, &per_sm));
     int64_t g = (op.sub.D + BLOCK - 1) / BLOCK;
-    const int64_t cap = (int64_t)sm_count() * occ_blocks;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
     if (g > cap) g = cap;
     kern<<<(int)(g < 1 ? 1 : g), BLOCK, smem, st>>>(op, static_cast<const V *>(x),
                                                    static_cast<V *>(y), err, gate, gate2);
@@ -698,11 +699,12 @@ template <typename V, int KB, int FM>
 int launch_hash(const rq_operator_t &op, const void *x, void *y, int *err, cudaStream_t st,
                 const int *gate, const int *gate2) {
     // small group sets: several 256-thread blocks per SM; large ones (streamed in tiles of
-    // kMaxResidentGroups above that count): one 1024-thread block.
-    // With the tag words the probes read 4 bytes per bucket (not with 64-bit keys and the bitset
-    // filter, whose tag kernel spills registers).
-    const bool small = op.terms.J <= kMaxResidentGroups && group_key_bytes<KB>(op.terms.J) <= 16 * 1024;
-    if (op.sub.htags && !(KB == 64 && FM == kFiltSet))
+    // max_resident_groups above that count): one 1024-thread block.
+    // With a line filter the probes test its bits (not with 64-bit keys and the bitset filter,
+    // whose line-filter kernel spills registers).
+    const bool small = op.terms.J <= max_resident_groups<KB>() &&
+                       group_key_bytes<KB>(op.terms.J) <= 16 * 1024;
+    if (op.sub.lmap && !(KB == 64 && FM == kFiltSet))
         return small ? launch_hash_block<V, KB, FM, 256, true>(op, x, y, err, st, gate, gate2)
                      : launch_hash_block<V, KB, FM, 1024, true>(op, x, y, err, st, gate, gate2);
     return small ? launch_hash_block<V, KB, FM, 256, false>(op, x, y, err, st, gate, gate2)
@@ -719,22 +721,11 @@ int launch_free(const rq_operator_t &op, const void *x, void *y, int stop_at_zer
     const size_t smem = kFilterBytes + (LK == RQ_LOOKUP_BSEARCH ? kSample * 8 : 0) +
                         tile_bytes<R>(gt, kt);
     auto kern = k_matvec_free<V, LK>;
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
-    // occupancy query cached per instantiation and shared-memory size (it is also reached while a
-    // stream is being captured, where only stream work should be issued)
-    static size_t occ_smem = ~size_t(0);
-    static int occ_blocks = 1;
-    if (occ_smem != smem) {
-        int per = 0;
-        RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, smem));
-        occ_blocks = per < 1 ? 1 : per;
-        occ_smem = smem;
-    }
-    const int per_sm = occ_blocks;
+    thread_local KernelLaunchCache table[kMaxCachedDevices];
+    KernelLaunchCache *c = nullptr;
+    int per_sm = 1;
+    RQ_TRY(cache_slot(table, &c));
+    RQ_TRY(configure_kernel(kern, *c, smem, kThreads, &per_sm));
     int64_t g = (op.sub.D + kThreads - 1) / kThreads;
     const int64_t cap = (int64_t)sm_count() * per_sm;
     if (g > cap) g = cap;

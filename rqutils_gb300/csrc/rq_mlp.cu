@@ -338,11 +338,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const GemmArgs g) {
 template <int N, int EPI>
 int launch_gemm(const GemmArgs &g, int64_t tiles, int64_t splits, cudaStream_t st) {
     constexpr uint32_t smem = gemm_smem_bytes<N>();
-    static bool configured = false;  // one GPU per process
-    if (!configured) {
-        RQ_CUDA(cudaFuncSetAttribute(k_gemm<N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    thread_local KernelLaunchCache table[kMaxCachedDevices];
+    KernelLaunchCache *c = nullptr;
+    int per_sm = 1;
+    RQ_TRY(cache_slot(table, &c));
+    RQ_TRY(configure_kernel(k_gemm<N, EPI>, *c, smem, kGemmThreads, &per_sm));
     if (tiles < 1 || splits < 1 || tiles > 0x7FFFFFFF || splits > 65535)
         return fail(RQ_E_RANGE, "bf16 GEMM: grid out of range");
     k_gemm<N, EPI><<<dim3((unsigned)tiles, (unsigned)splits), kGemmThreads, smem, st>>>(g);

@@ -92,33 +92,38 @@ k_hash_insert(const uint64_t *__restrict__ states, int64_t D, void *keys, int32_
     }
 }
 
-// Tag word of each bucket, one thread per bucket: the tags of slots 0 and 1 (0 for an empty slot,
-// else 0x8000 for a key in its home bucket or 0x4000 for a key moved on from a full bucket, | the
-// low 13 bits of the key's hash) and the "more keys" bit when slot 2 is occupied.  A probe compares
-// its target's tag with the word and reads the keys only when it matches or has more keys.
+// Highest differing bit of neighbouring sorted states: hist[h] counts the i with
+// 63 - clz(s[i] ^ s[i - 1]) == h.  The number of distinct prefixes s >> b is then
+// 1 + sum_{h >= b} hist[h] for every b at once.
+__global__ void k_prefix_hist(const uint64_t *__restrict__ s, int64_t D,
+                              unsigned long long *__restrict__ hist) {
+    __shared__ unsigned int h[64];
+    if (threadIdx.x < 64) h[threadIdx.x] = 0u;
+    __syncthreads();
+    for (int64_t i = 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
+         i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[63 - __clzll((long long)(s[i] ^ s[i - 1]))], 1u);
+    __syncthreads();
+    if (threadIdx.x < 64 && h[threadIdx.x]) atomicAdd(hist + threadIdx.x, (unsigned long long)h[threadIdx.x]);
+}
+
+// Line filter: for every state, bit (hash(s) mod 2^lwbits) of line hash(s >> lshift) >> (32 -
+// lbits).  Both hashes are the GF(2)-linear lookup hash, so a target's line and bit follow from
+// the row's and the X mask's by XOR.
 template <int KB>
 __global__ void __launch_bounds__(kThreads)
-k_tag_fill(const void *__restrict__ keys, int hbits, uint64_t empty, uint32_t *__restrict__ tags) {
-    using K = typename KeyWidth<KB>::K;
+k_line_build(const uint64_t *__restrict__ s, int64_t D, uint32_t *__restrict__ lmap, int lbits,
+             int lwbits, int lshift) {
     __shared__ uint32_t T[kHashTableWords];
     init_hash_tables(T, KeyWidth<KB>::kNbytes);
     __syncthreads();
-    const int64_t nb = int64_t(1) << hbits;
-    const K *kk = static_cast<const K *>(keys);
-    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb;
-         b += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t w = 0u;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const K k = kk[b * kBucketSlots + s];
-            if (k == (K)empty) continue;
-            const uint32_t h = lin_hash(T, (uint64_t)k, KeyWidth<KB>::kNbytes);
-            const uint32_t home = bucket_from_hash(h, hbits);
-            const uint32_t tag = (home == (uint32_t)b ? kTagHome : kTagMoved) | (h & kTagMask);
-            w |= tag << (16 * s);
-        }
-        if (kk[b * kBucketSlots + 2] != (K)empty) w |= kTagMore;
-        tags[b] = w;
+    const uint32_t bmask = (1u << lwbits) - 1u;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = s[i];
+        const uint32_t line = lin_hash(T, lshift < 64 ? k >> lshift : 0ULL, KeyWidth<KB>::kNbytes) >> (32 - lbits);
+        const uint32_t bit = lin_hash(T, k, KeyWidth<KB>::kNbytes) & bmask;
+        atomicOr(lmap + ((size_t)line << (lwbits - 5)) + (bit >> 5), 1u << (bit & 31));
     }
 }
 
@@ -306,6 +311,18 @@ RQ_API int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits) {
     return RQ_OK;
 }
 
+RQ_API int rq_line_filter_bits(int64_t D, int32_t lwbits, int32_t *lbits) {
+    if (!lbits || D < 1 || lwbits < 8 || lwbits > 10)
+        return fail(RQ_E_ARG, "rq_line_filter_bits: D >= 1 and 8 <= lwbits <= 10");
+    const int64_t per = int64_t(1) << (lwbits - 7);  // states per line on average
+    const int64_t lines = (D + per - 1) / per;
+    int b = 1;
+    while ((int64_t(1) << b) < lines) ++b;
+    if (b > 31) return fail(RQ_E_RANGE, "rq_line_filter_bits: D too large");
+    *lbits = b;
+    return RQ_OK;
+}
+
 RQ_API int rq_presence_bits(int64_t D, int32_t key_bits, int32_t *pbits) {
     if (!pbits) return fail(RQ_E_ARG, "rq_presence_bits: null argument");
     int32_t hb = 0;
@@ -336,6 +353,9 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     cudaStream_t st = as_stream(stream);
     int *flag = scratch_err(scratch);
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
+    if (sub->lookup == RQ_LOOKUP_HASH && sub->lmap &&
+        (sub->lbits < 1 || sub->lbits > 31 || sub->lwbits < 8 || sub->lwbits > 10))
+        return fail(RQ_E_ARG, "rq_subspace_build: line filter needs 1 <= lbits <= 31, 8 <= lwbits <= 10");
     if (sub->lookup == RQ_LOOKUP_HASH && sub->pbits != 0 &&
         (!sub->pmap || sub->pbits < 5 || sub->pbits > 32 || sub->pbits < sub->hbits))
         return fail(RQ_E_ARG, "rq_subspace_build: presence bitmap missing or pbits out of range");
@@ -343,13 +363,36 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
                                    sub->hkeys, sub->hvals, sub->hbits, &sub->empty_key, flag, gap,
                                    st, sub->pbits ? sub->pmap : nullptr, sub->pbits);
     if (rc != RQ_OK) return fail(rc, std::string("rq_subspace_build: ") + rq_last_error());
-    if (sub->lookup == RQ_LOOKUP_HASH && sub->htags) {
-        const int g = grid_for(int64_t(1) << sub->hbits);
-        uint32_t *tags = sub->htags;
+    if (sub->lookup == RQ_LOOKUP_HASH && sub->lmap) {
+        // prefix shift: the largest b with about 2^(lwbits - 5) states per distinct s >> b
+        // (the histogram sits in the reduction partials of the scratch, past the reduction
+        // counter, which must stay zero)
+        unsigned long long *hist = reinterpret_cast<unsigned long long *>(
+            static_cast<char *>(scratch_reduce(scratch)) + 16);
+        RQ_CUDA(cudaMemsetAsync(hist, 0, 64 * sizeof(unsigned long long), st));
+        k_prefix_hist<<<grid_for(D), kThreads, 0, st>>>(sub->states, D, hist);
+        RQ_CUDA(cudaGetLastError());
+        unsigned long long h[64];
+        RQ_CUDA(cudaMemcpyAsync(h, hist, sizeof(h), cudaMemcpyDeviceToHost, st));
+        RQ_CUDA(cudaStreamSynchronize(st));
+        const double per = (double)(1 << (sub->lwbits - 5));
+        int b = 0;
+        unsigned long long above = 0;  // distinct prefixes at shift b, minus one
+        for (int k = 63; k >= 0; --k) above += h[k];
+        for (int c = 1; c <= sub->key_bits; ++c) {
+            above -= h[c - 1];
+            if ((double)D > per * (double)(above + 1)) break;
+            b = c;
+        }
+        sub->lshift = b;
+        const size_t bytes = (size_t)1 << (sub->lbits + sub->lwbits - 3);
+        RQ_CUDA(cudaMemsetAsync(sub->lmap, 0, bytes, st));
         if (sub->key_bits == 64)
-            k_tag_fill<64><<<g, kThreads, 0, st>>>(sub->hkeys, sub->hbits, sub->empty_key, tags);
+            k_line_build<64><<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->lmap,
+                                                                sub->lbits, sub->lwbits, b);
         else
-            k_tag_fill<32><<<g, kThreads, 0, st>>>(sub->hkeys, sub->hbits, sub->empty_key, tags);
+            k_line_build<32><<<grid_for(D), kThreads, 0, st>>>(sub->states, D, sub->lmap,
+                                                                sub->lbits, sub->lwbits, b);
         RQ_CUDA(cudaGetLastError());
     }
     RQ_CUDA(cudaMemsetAsync(sub->fbits, 0, RQ_FILTER_WORDS * sizeof(uint32_t), st));

@@ -3,10 +3,12 @@
 // X / Z masks (bit q = qubit q).
 //
 //   1. drop exact-zero coefficients (symplectic.py:68-69);
-//   2. merge equal strings (symplectic.py:70-73: np.unique of the labels and np.add.at of their
-//      coefficients): a stable radix sort of the term indices by the string's lexicographic key
+//   2. merge equal strings (symplectic.py:70-73: np.unique of the labels, the coefficients of a
+//      label summed): a stable radix sort of the term indices by the string's lexicographic key
 //      (character 0 = qubit n-1, I < X < Y < Z, i.e. the 2-bit code 2 z + (x ^ z) per qubit), then
-//      one thread per run of equal keys adds the run's coefficients from 0 in input order;
+//      one thread per run of equal keys adds the run's coefficients from 0 in input order (the
+//      reference sums through a matrix product, masks @ coeffs, whose order is the BLAS
+//      library's: a merged duplicate can differ from it in the last bit);
 //   3. force_real: the merged coefficients' real parts (symplectic.py:93-96);
 //   4. group by X mask in ascending order, members in string order (symplectic.py:99-108): a
 //      stable radix sort of the merged terms by X mask;

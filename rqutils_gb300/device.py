@@ -62,11 +62,11 @@ class DeviceSubspace:
     """Sorted distinct states (uint64, bit q = qubit q) with their lookup structures."""
 
     def __init__(self, states, num_qubits=64, lookup='hash', filter_masks=None, device=None,
-                 stream=None, key_bits=None, presence=None, tags=True):
+                 stream=None, key_bits=None, presence=None, line_filter=True, line_bits=8):
         """``presence``: None = a presence bitmap when the hash table does not fit in L2
-        (rq_presence_bits), False = none, an int = its size log2.  ``tags``: build the 4-byte tag
-        word of every bucket, which the matrix-free kernel probes instead of the key buckets
-        (same results; False probes the key buckets)."""
+        (rq_presence_bits), False = none, an int = its size log2.  ``line_filter``: build the
+        line filter (lines of 2^line_bits bits, 8..10) that the matrix-free kernel probes before
+        the key buckets (same results; False probes the key buckets directly)."""
         self.device = device or default_device()
         if isinstance(states, torch.Tensor):
             self.states = states.to(self.device, dtype=torch.int64).contiguous()
@@ -91,11 +91,16 @@ class DeviceSubspace:
             self.hkeys = torch.empty((4 * key_bits // 64) << self.hbits, dtype=torch.int64,
                                      device=self.device)
             self.hvals = torch.empty(4 << self.hbits, dtype=torch.int32, device=self.device)
-            # one 4-byte tag word per bucket, probed by the matrix-free kernel
-            self.htags = (torch.empty(1 << self.hbits, dtype=torch.int32, device=self.device)
-                          if tags else None)
         else:
-            self.hkeys = self.hvals = self.htags = None
+            self.hkeys = self.hvals = None
+        self.lmap, self.lbits, self.lwbits = None, 0, 0
+        if self.lookup == L.LOOKUP_HASH and line_filter:
+            lb = ctypes.c_int32()
+            L.check(L.lib().rq_line_filter_bits(self.D, int(line_bits), ctypes.byref(lb)),
+                    'rq_line_filter_bits')
+            self.lbits, self.lwbits = lb.value, int(line_bits)
+            self.lmap = torch.empty(1 << (self.lbits + self.lwbits - 5), dtype=torch.int32,
+                                    device=self.device)
         self.fbits = torch.zeros(L.FILTER_WORDS, dtype=torch.int32, device=self.device)
         # presence bitmap in front of a hash table too large for L2
         self.pbits = 0
@@ -114,7 +119,8 @@ class DeviceSubspace:
                             hvals=L.ptr(self.hvals), hbits=self.hbits, lookup=self.lookup,
                             key_bits=key_bits, pbits=self.pbits, empty_key=0, fmask_a=int(fa),
                             fmask_b=int(fb), fbits=L.ptr(self.fbits), pmap=L.ptr(self.pmap),
-                            htags=L.ptr(self.htags), fpoint=-1)
+                            lmap=L.ptr(self.lmap), lbits=self.lbits, lwbits=self.lwbits,
+                            lshift=0, fpoint=-1)
         L.check(L.lib().rq_subspace_build(ctypes.byref(self.c), L.ptr(self.scratch),
                                           L.stream_ptr(stream)), 'rq_subspace_build')
 

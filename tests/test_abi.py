@@ -68,9 +68,9 @@ def test_host_only_entry_points(libpath):
 
 def test_struct_layouts():
     from rqutils_gb300 import _lib as L
-    assert ctypes.sizeof(L.Subspace) == 104
+    assert ctypes.sizeof(L.Subspace) == 112
     assert ctypes.sizeof(L.Terms) == 56
-    assert ctypes.sizeof(L.Operator) == 104 + 56 + 8 + 40 + 8
+    assert ctypes.sizeof(L.Operator) == 112 + 56 + 8 + 40 + 8
     assert ctypes.sizeof(L.LobpcgParams) == 64
     assert ctypes.sizeof(L.LobpcgResult) == 48
     assert ctypes.sizeof(L.Batch) == 208

@@ -313,14 +313,14 @@ def test_persistent_loop_matches_graph_loop(cache_level, variant):
         assert abs(torch.vdot(x1, x2).item()) > 1 - 1e-10
 
 
-@pytest.mark.parametrize('tags', [True, False])
+@pytest.mark.parametrize('line', [True, False])
 @pytest.mark.parametrize('key_bits', [32, 64])
 @pytest.mark.parametrize('sectors', ['one', 'two', 'off'])
-def test_hash_kernel_sector_filter_modes(sectors, key_bits, tags):
+def test_hash_kernel_sector_filter_modes(sectors, key_bits, line):
     """The FREE hash kernel's three filter forms -- a subspace in one (popcount a, popcount b)
     sector (two popcount compares), several sectors (the bitset) and the filter off -- give the
-    oracle's product, and all three agree bit for bit with each other, probing the tag words or
-    the key buckets."""
+    oracle's product, and all three agree bit for bit with each other, probing through the line
+    filter or the key buckets directly."""
     import torch
     from oracle import sqd as osqd
     from oracle.paulis import from_paulisum as oterms
@@ -340,7 +340,7 @@ def test_hash_kernel_sector_filter_modes(sectors, key_bits, tags):
     v = workloads.random_vector(rng, len(S))
     ref = osqd.matvec_xcached(v, osqd.xsources_all(S, ot), ot, S)
     fm = (0, 0) if sectors == 'off' else None
-    sub = DeviceSubspace(S, num_qubits=n, filter_masks=fm, key_bits=key_bits, tags=tags)
+    sub = DeviceSubspace(S, num_qubits=n, filter_masks=fm, key_bits=key_bits, line_filter=line)
     bits = int(np.bitwise_count(sub.fbits.cpu().numpy().view(np.uint32)).sum())
     assert bits == {'one': 1, 'two': 2, 'off': bits}[sectors]
     assert (sub.c.fpoint >= 0) == (sectors == 'one')
@@ -349,17 +349,18 @@ def test_hash_kernel_sector_filter_modes(sectors, key_bits, tags):
     op.check_errors()
     assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref)
     other = DeviceSubspace(S, num_qubits=n, filter_masks=(0, 0), key_bits=key_bits,
-                           tags=not tags)
+                           line_filter=not line)
     y0 = DeviceOperator(DeviceTerms(h), other, mode='free').matvec(torch.as_tensor(v).cuda()).cpu().numpy()
     np.testing.assert_array_equal(y, y0)
 
 
+@pytest.mark.parametrize('line_bits', [8, 10])
 @pytest.mark.parametrize('key_bits', [32, 64])
 @pytest.mark.parametrize('dtype', ['float32', 'float64', 'complex64', 'complex128'])
-def test_tag_words_match_key_buckets(key_bits, dtype):
+def test_line_filter_matches_key_buckets(key_bits, dtype, line_bits):
     """2^16 states (buckets with three or four keys and keys moved on from full buckets occur):
-    the matrix-free product through the tag words equals, bit for bit, the product through the
-    key buckets and the cached-connectivity product."""
+    the matrix-free product through the line filter equals, bit for bit, the product through the
+    key buckets and the cached-connectivity product; every state's bit is set."""
     import torch
     from rqutils_gb300 import workloads
     from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
@@ -370,26 +371,26 @@ def test_tag_words_match_key_buckets(key_bits, dtype):
     S = workloads.sample_sector(rng, 1 << 16, [(12, 6), (12, 6)])
     h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
     terms = DeviceTerms(h)
-    with_tags = DeviceSubspace(S, num_qubits=n, key_bits=key_bits)
-    words = with_tags.htags.cpu().numpy().view(np.uint32)
-    assert (words & 0x20000000).any()                          # a bucket with three keys or more
-    halves = np.concatenate([words & 0xFFFF, words >> 16])
-    assert ((halves & 0xC000) == 0x4000).any()                 # a key moved on from a full bucket
-    no_tags = DeviceSubspace(S, num_qubits=n, key_bits=key_bits, tags=False)
+    lf = DeviceSubspace(S, num_qubits=n, key_bits=key_bits, line_bits=line_bits)
+    assert 0 < lf.c.lshift <= key_bits
+    words = lf.lmap.cpu().numpy().view(np.uint32)
+    ones = int(np.bitwise_count(words).sum())
+    assert 0 < ones <= len(S)                          # one bit per state, some shared
+    plain = DeviceSubspace(S, num_qubits=n, key_bits=key_bits, line_filter=False)
     dt = getattr(torch, dtype)
     if not dt.is_complex and not terms.is_real:
         pytest.skip('complex coefficients need complex vectors')
     x = torch.as_tensor(rng.normal(size=len(S)) + 1j * rng.normal(size=len(S)))
     x = (x if dt.is_complex else x.real).to(dt).cuda()
-    a = DeviceOperator(terms, with_tags, mode='free')
+    a = DeviceOperator(terms, lf, mode='free')
     y = a.matvec(x)
     a.check_errors()
-    assert torch.equal(y, DeviceOperator(terms, no_tags, mode='free').matvec(x))
-    assert torch.equal(y, DeviceOperator(terms, with_tags, mode='conn').matvec(x))
+    assert torch.equal(y, DeviceOperator(terms, plain, mode='free').matvec(x))
+    assert torch.equal(y, DeviceOperator(terms, lf, mode='conn').matvec(x))
 
 
-@pytest.mark.parametrize('tags', [True, False])
-def test_hash_kernel_streams_more_than_16384_groups(tags):
+@pytest.mark.parametrize('line', [True, False])
+def test_hash_kernel_streams_more_than_16384_groups(line):
     """A Pauli sum with more X groups than shared memory holds (the group keys are streamed in
     tiles): the matrix-free product equals the oracle's row-by-row product and, bit for bit, the
     cached-connectivity product."""
@@ -410,10 +411,68 @@ def test_hash_kernel_streams_more_than_16384_groups(tags):
     ref, hits = osqd.rows_matvec(v, ot, S, np.arange(len(S)))
     assert sum(len(r) for r in hits) > 1000
     terms = DeviceTerms(h)
-    sub = DeviceSubspace(S, num_qubits=n, tags=tags)
+    sub = DeviceSubspace(S, num_qubits=n, line_filter=line)
     free = DeviceOperator(terms, sub, mode='free')
     y = free.matvec(torch.as_tensor(v).cuda())
     free.check_errors()
     yh = y.cpu().numpy()
     assert np.linalg.norm(yh - ref) <= 1e-12 * np.linalg.norm(ref)
     assert torch.equal(y, DeviceOperator(terms, sub, mode='conn').matvec(torch.as_tensor(v).cuda()))
+
+
+@pytest.mark.parametrize('variant', ['reference', 'fast'])
+def test_start_almost_inside_a_two_dimensional_invariant_subspace(variant):
+    """A diagonal Hamiltonian (Z terms only) from x0 = e_a + 2 e_b + 1e-9 e_c: at first the new
+    search direction lies inside span(x, y) up to a relative 1e-9, where a norm taken from inner
+    products is only rounding; the solver must still return the lowest of the three diagonal
+    values, not a Rayleigh-Ritz value of a mis-scaled basis."""
+    import torch
+    from rqutils_gb300.ground_locg import lobpcg_solve
+    from rqutils_gb300.sqd import SQDProblem
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    n = 6
+    rng = np.random.default_rng(77)
+    labels = [''.join(rng.choice(['I', 'Z'], size=n)) for _ in range(12)]
+    h = PauliSumXZ.from_paulisum((labels, rng.normal(size=12)), force_real=True, add_padding=True)
+    S = np.arange(1 << n, dtype=np.uint64)
+    prob = SQDProblem(h, S, cache_level=(1, 0))
+    d = prob.op.diag0.cpu().numpy()
+    order = np.argsort(d)
+    a, b, c = int(order[5]), int(order[9]), int(order[20])   # c above a and b
+    assert d[a] < d[b] < d[c]
+    x0 = np.zeros(1 << n)
+    x0[a], x0[b], x0[c] = 1., 2., 1e-9
+    eig, x, info = lobpcg_solve(prob.op, torch.as_tensor(x0).cuda(), maxiter=200,
+                                variant=variant, target_rel=1e-10)
+    assert np.isfinite(eig)
+    assert abs(eig - d[a]) <= 1e-10 * max(1., abs(d[a])), (eig, d[a], d[b], d[c])
+    assert abs(abs(x.cpu().numpy()[a]) - 1.) < 1e-8
+
+
+def test_32bit_keys_with_x_masks_above_bit_31():
+    """32-bit keys (every state below 2^32) with a Pauli sum on 40 qubits: targets S[i] ^ x with
+    bits at or above 32 are never states, even where their low 32 bits equal one; the products
+    equal the oracle's."""
+    import torch
+    from oracle import sqd as osqd
+    from oracle.paulis import from_paulisum as oterms
+    from rqutils_gb300 import workloads
+    from rqutils_gb300.device import DeviceOperator, DeviceSubspace, DeviceTerms
+    from rqutils_gb300.paulis.symplectic import PauliSumXZ
+    rng = np.random.default_rng(808)
+    labels, coeffs = workloads.random_pauli_masks(rng, 40, 600, locality=(1, 4))
+    # terms whose X part has bits at or above 32 and whose low half alone connects states
+    hi = ['X' * 2 + 'I' * 6 + lab[8:] for lab in labels[:200]]
+    labels, coeffs = list(labels) + hi, np.concatenate([coeffs, rng.normal(size=200)])
+    S = workloads.sample_sector(rng, 4000, [(16, 8), (16, 8)])
+    h = PauliSumXZ.from_paulisum((labels, coeffs), force_real=True, add_padding=True)
+    ot = oterms((labels, coeffs), force_real=True)
+    assert any(int(x) >> 32 for x in h.xmask)
+    terms = DeviceTerms(h)
+    sub = DeviceSubspace(S, num_qubits=32, key_bits=32)
+    v = workloads.random_vector(rng, len(S))
+    ref, _ = osqd.rows_matvec(v, ot, S, np.arange(len(S)))
+    for mode in ('free', 'conn'):
+        op = DeviceOperator(terms, sub, mode=mode)
+        y = op.matvec(torch.as_tensor(v).cuda()).cpu().numpy()
+        assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref), mode
