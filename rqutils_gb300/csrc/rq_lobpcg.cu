@@ -14,6 +14,7 @@
 // update (four matvecs), as the reference does; FAST carries A x and A y by linearity (one matvec
 // per iteration) and recomputes them every `refresh` iterations and before accepting convergence.
 // Mixed precision runs a 32-bit phase first and continues in the 64-bit type from its x and y.
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <algorithm>
@@ -1064,6 +1065,8 @@ struct MvCallback {
     }
 };
 
+struct BatchPersist;  // the persistent batched solve's plan (below)
+
 template <typename V, typename SEG, typename MV>
 struct Phase {
     MV mv;
@@ -1080,6 +1083,8 @@ struct Phase {
     // connectivity or CSR operator of this phase's value type)
     const rq_operator_t *pop = nullptr;
     GridBar *bar = nullptr;
+    // set when a batched loop may run as persistent launches (cached-connectivity batches)
+    BatchPersist *bp = nullptr;
     // optional: shrink the block list to the problems still active (active > 0) or restore the
     // full list (active < 0); sets `grid`
     int (*compact)(void *ctx, int active, int *grid, cudaStream_t s) = nullptr;
@@ -1262,12 +1267,12 @@ constexpr long long kBarrierCycles = 4000000000LL;  // ~2 s at 2 GHz: a barrier 
 // reaches (barriers passed) x (blocks); `passed` is the block's own count, kept in shared
 // memory.  Every wait is bounded; a block that gives up raises `abort`, which releases every
 // other waiter at once.  Returns false after an abort.
-__device__ bool grid_sync(GridBar *b, unsigned int *passed) {
+__device__ bool group_sync(GridBar *b, unsigned int *passed, unsigned int nblocks) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned int target = (*passed + 1u) * gridDim.x;
+        const unsigned int target = (*passed + 1u) * nblocks;
         *passed += 1u;
         volatile unsigned int *count = &b->count;
         volatile int *abort = &b->abort;
@@ -1291,6 +1296,11 @@ __device__ bool grid_sync(GridBar *b, unsigned int *passed) {
     }
     __syncthreads();
     return ok_s != 0;
+}
+
+// Barrier over the whole grid.
+__device__ __forceinline__ bool grid_sync(GridBar *b, unsigned int *passed) {
+    return group_sync(b, passed, gridDim.x);
 }
 
 // One problem inside the persistent kernel: every block holds its own copy of the solver state
@@ -1337,6 +1347,48 @@ struct SegPersist {
     }
 };
 
+// One problem of a batch inside the persistent batched kernel: blocks [b0, b0 + nb) of the grid
+// (this block is number lb of them) own the problem's rows [r0, r1), reduce into the problem's
+// own partial sums and cross the problem's own barrier; otherwise as SegPersist.
+struct SegPersistB {
+    State *st;
+    int64_t r0, r1;
+    int lb, nb;
+    float4 *part;           // [2][nb * kMaxReduce]
+    GridBar *bar;
+    int *flip;
+    unsigned int *passed;
+    __device__ __forceinline__ State *state() const { return st; }
+    __device__ __forceinline__ int64_t begin() const {
+        return r0 + (int64_t)lb * blockDim.x + threadIdx.x;
+    }
+    __device__ __forceinline__ int64_t end() const { return r1; }
+    __device__ __forceinline__ int64_t stride() const { return (int64_t)nb * blockDim.x; }
+    template <int NV>
+    __device__ void reduce(cdf (&v)[NV], int slot) const {
+        __shared__ cdf red[kThreads / 32][NV];
+        __shared__ cdf tot[NV];
+        cdf w[NV];
+        float4 *pb = part + (size_t)(*flip) * nb * kMaxReduce;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) w[k] = v[k];
+        block_sum_all<NV>(w, tot, red);
+        if (threadIdx.x < NV) {
+            pb[(size_t)lb * kMaxReduce + threadIdx.x] = cdf_pack(tot[threadIdx.x]);
+            __threadfence();
+        }
+        if (!group_sync(bar, passed, (unsigned int)nb)) {
+            if (threadIdx.x == 0) st->active = 0;
+            __syncthreads();
+            return;
+        }
+        partials_sum<NV>(pb, nb, kMaxReduce, tot);
+        if (threadIdx.x < NV) st->red[slot + threadIdx.x] = cdf_val(tot[threadIdx.x]);
+        if (threadIdx.x == 0) *flip ^= 1;
+        __syncthreads();
+    }
+};
+
 template <typename V>
 struct PersistArgs {
     State *st;      // global state (read at start, written back by block 0 at the end)
@@ -1360,6 +1412,81 @@ __device__ __forceinline__ void persist_mv(const PersistArgs<V> &a, State *st, c
         d_matvec_csr<V, V>(a.op, in, out, &st->active, gate2);
 }
 
+// The iterations of one phase inside a persistent kernel (ground_locg.py:288-341): the passes
+// of Phase::iteration, separated by barriers of the segment instead of kernel boundaries.
+// mv(in, out, gate2) forms a product over the segment's rows; sync() crosses the segment's
+// barrier and returns false after an abort; the loop also ends at iteration stop_iter.  Element
+// i is always handled by the same thread, so passes that only touch a thread's own elements need
+// no barrier; barriers stand before the products (which gather rows of other blocks) and inside
+// every reduction.
+template <typename V, typename SEG, typename MVF, typename SYNC>
+__device__ __forceinline__ void persist_loop(const SEG &seg, State *st, const Vecs<V> &v,
+                                             int variant, int jacobi, const double *diag, MVF &mv,
+                                             SYNC &sync, int stop_iter) {
+    constexpr int kOnce = 1 << 30;  // step of the scalar loops: thread 0 only
+    auto scalar_done = [&]() { __syncthreads(); };
+    while (st->active && st->iter < stop_iter) {
+        V *src = v.r;
+        if (jacobi) {
+            d_jacobi<V, SEG>(seg, diag, v.r, v.w);
+            src = v.w;
+        }
+        // project_out((x, y), src) -> p
+        if (variant == RQ_LOBPCG_FAST) {
+            Pairs<V, 6> g{{v.x, v.y, v.x, v.x, v.y, src}, {src, src, v.x, v.y, v.y, src}};
+            d_dots<V, 6, SEG>(seg, g, kG10);
+            if (threadIdx.x == 0) d_proj_coef(st, 1, 0, kOnce);
+            scalar_done();
+            d_sub2_scale<V, SEG>(seg, v.x, v.y, src, v.p);
+        } else {
+            Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
+            d_dots<V, 2, SEG>(seg, pr, kIp0);
+            d_sub2_norm<V, SEG>(seg, v.x, v.y, src);
+            d_scale_dots2<V, SEG>(seg, v.x, v.y, src, 1);
+            d_sub2_norm<V, SEG>(seg, v.x, v.y, src);
+            d_scale_dots2<V, SEG>(seg, v.x, v.y, src, 1);
+            d_sub2_norm<V, SEG>(seg, v.x, v.y, src);
+            d_scale_dots2<V, SEG>(seg, v.x, v.y, src, 0);
+            d_sub2_norm<V, SEG>(seg, v.x, v.y, src);
+            d_mask<V, SEG>(seg, src, v.p);
+        }
+        if (!sync()) break;  // the products gather p (and x, y) from every block's rows
+        if (variant == RQ_LOBPCG_REFERENCE) {
+            mv(v.x, v.ax, nullptr);
+            mv(v.y, v.ay, nullptr);
+        }
+        mv(v.p, v.ap, nullptr);
+        d_gram3<V, SEG>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+        if (threadIdx.x == 0) d_rr3(st, 1, 0, kOnce);
+        scalar_done();
+        if (variant == RQ_LOBPCG_FAST) {
+            d_upd_stu<V, SEG>(seg, v.x, v.y, v.p);
+            if (threadIdx.x == 0) d_stu_coef(st, 1, 0, kOnce);
+            scalar_done();
+        } else {
+            d_upd_s<V, SEG>(seg, v.y, v.p);
+            d_upd_tu<V, SEG>(seg, v.x, v.y, v.p);
+        }
+        if (variant == RQ_LOBPCG_REFERENCE) {
+            d_upd_xy<V, false, SEG>(seg, v.x, v.y, v.p, nullptr, nullptr, nullptr);
+            if (!sync()) break;
+            mv(v.x, v.ax, nullptr);
+        } else {
+            d_upd_xy<V, true, SEG>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
+            if (st->want_refresh) {
+                if (!sync()) break;
+                mv(v.x, v.ax, &st->want_refresh);
+                mv(v.y, v.ay, &st->want_refresh);
+                if (threadIdx.x == 0) d_refresh_mark(st, 1, 0, kOnce);
+                scalar_done();
+            }
+        }
+        d_resid<V, SEG>(seg, v.ax, v.x, v.r, 0);
+        if (threadIdx.x == 0) d_check(st, 1, nullptr, 0, kOnce);
+        scalar_done();
+    }
+}
+
 template <typename V, int MVK>
 __global__ void __launch_bounds__(kThreads) k_persist(const PersistArgs<V> a) {
     __shared__ State sst;
@@ -1377,80 +1504,96 @@ __global__ void __launch_bounds__(kThreads) k_persist(const PersistArgs<V> a) {
     __syncthreads();
     State *st = &sst;
     const SegPersist seg{st, a.D, a.part, a.bar, &flip, &passed};
-    const Vecs<V> v = a.v;
-    constexpr int kOnce = 1 << 30;  // step of the scalar loops: thread 0 only
     auto sync = [&]() -> bool {
         if (grid_sync(a.bar, &passed)) return true;
         if (threadIdx.x == 0) st->active = 0;
         __syncthreads();
         return false;
     };
-    auto scalar_done = [&]() { __syncthreads(); };
-    while (st->active) {
-        V *src = v.r;
-        if (a.jacobi) {
-            d_jacobi<V, SegPersist>(seg, a.diag, v.r, v.w);
-            src = v.w;
-        }
-        // project_out((x, y), src) -> p
-        if (a.variant == RQ_LOBPCG_FAST) {
-            Pairs<V, 6> g{{v.x, v.y, v.x, v.x, v.y, src}, {src, src, v.x, v.y, v.y, src}};
-            d_dots<V, 6, SegPersist>(seg, g, kG10);
-            if (threadIdx.x == 0) d_proj_coef(st, 1, 0, kOnce);
-            scalar_done();
-            d_sub2_scale<V, SegPersist>(seg, v.x, v.y, src, v.p);
-        } else {
-            Pairs<V, 2> pr{{v.x, v.y}, {src, src}};
-            d_dots<V, 2, SegPersist>(seg, pr, kIp0);
-            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-            d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
-            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-            d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 1);
-            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-            d_scale_dots2<V, SegPersist>(seg, v.x, v.y, src, 0);
-            d_sub2_norm<V, SegPersist>(seg, v.x, v.y, src);
-            d_mask<V, SegPersist>(seg, src, v.p);
-        }
-        if (!sync()) break;  // the products gather p (and x, y) from every block's rows
-        if (a.variant == RQ_LOBPCG_REFERENCE) {
-            persist_mv<V, MVK>(a, st, v.x, v.ax, nullptr);
-            persist_mv<V, MVK>(a, st, v.y, v.ay, nullptr);
-        }
-        persist_mv<V, MVK>(a, st, v.p, v.ap, nullptr);
-        d_gram3<V, SegPersist>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
-        if (threadIdx.x == 0) d_rr3(st, 1, 0, kOnce);
-        scalar_done();
-        if (a.variant == RQ_LOBPCG_FAST) {
-            d_upd_stu<V, SegPersist>(seg, v.x, v.y, v.p);
-            if (threadIdx.x == 0) d_stu_coef(st, 1, 0, kOnce);
-            scalar_done();
-        } else {
-            d_upd_s<V, SegPersist>(seg, v.y, v.p);
-            d_upd_tu<V, SegPersist>(seg, v.x, v.y, v.p);
-        }
-        if (a.variant == RQ_LOBPCG_REFERENCE) {
-            d_upd_xy<V, false, SegPersist>(seg, v.x, v.y, v.p, nullptr, nullptr, nullptr);
-            if (!sync()) break;
-            persist_mv<V, MVK>(a, st, v.x, v.ax, nullptr);
-        } else {
-            d_upd_xy<V, true, SegPersist>(seg, v.x, v.y, v.p, v.ax, v.ay, v.ap);
-            if (st->want_refresh) {
-                if (!sync()) break;
-                persist_mv<V, MVK>(a, st, v.x, v.ax, &st->want_refresh);
-                persist_mv<V, MVK>(a, st, v.y, v.ay, &st->want_refresh);
-                if (threadIdx.x == 0) d_refresh_mark(st, 1, 0, kOnce);
-                scalar_done();
-            }
-        }
-        d_resid<V, SegPersist>(seg, v.ax, v.x, v.r, 0);
-        if (threadIdx.x == 0) d_check(st, 1, nullptr, 0, kOnce);
-        scalar_done();
-    }
+    auto mv = [&](const V *in, V *out, const int *gate2) { persist_mv<V, MVK>(a, st, in, out, gate2); };
+    persist_loop<V, SegPersist>(seg, st, a.v, a.variant, a.jacobi, a.diag, mv, sync, INT_MAX);
     // the copies are identical; block 0 publishes its own
     if (blockIdx.x == 0) {
         const int n = (int)(sizeof(State) / sizeof(int));
         for (int k = threadIdx.x; k < n; k += blockDim.x)
             reinterpret_cast<int *>(a.st)[k] = reinterpret_cast<const int *>(&sst)[k];
+    }
+}
+
+// The batched cached-connectivity product over one problem's rows (the batch matvec's CONN form
+// restricted to the segment): y[i] = diag0[i] x[i] + the row's cached (source, group) terms.
+template <typename V>
+__device__ __forceinline__ void d_batch_conn_seg(const rq_batch_t &B, const SegPersistB &seg,
+                                                 const V *x, V *y, const int *gate2) {
+    using R = typename VT<V>::R;
+    if (!seg.st->active || (gate2 && *gate2 == 0)) return;
+    constexpr uint64_t kMask = (1ULL << RQ_BATCH_STATE_BITS) - 1ULL;
+    SEG_LOOP(i) {
+        const uint64_t s = __ldg(B.keys + i) & kMask;
+        CAcc<R> acc;
+        const cx<R> xi = VT<V>::ld(x, i);
+        const R dv = (R)B.diag0[i];
+        acc.add({dv * xi.re, dv * xi.im});
+        const int64_t e1 = B.rowptr[i + 1];
+        for (int64_t e = B.rowptr[i]; e < e1; ++e)
+            acc.add(cmul(group_diag<R>(B.terms, __ldg(B.grp + e), s), VT<V>::ld(x, __ldg(B.col + e))));
+        VT<V>::st(y, i, acc.get());
+    }
+}
+
+template <typename V>
+struct PersistBatchArgs {
+    State *states;          // [P], read at start, written back by each problem's first block
+    rq_batch_t B;
+    Vecs<V> v;
+    int variant, jacobi;
+    const double *diag;
+    int iter_cap;           // iterations per problem in this launch
+    const int32_t *bprob;   // [grid] problem of each block
+    const int32_t *bfirst;  // [P] first block of each problem
+    const int32_t *nblk;    // [P] blocks of each problem
+    const int64_t *poff;    // [P] first float4 of each problem's partial sums
+    float4 *part;
+    GridBar *bars;          // [P]
+};
+
+// Many problems in one cooperative launch: each problem owns a group of blocks and runs
+// persist_loop on its own rows with its own reductions and barrier (blocks of different problems
+// never wait for each other), at most iter_cap iterations, after which the host re-plans the
+// block groups over the problems still active.
+template <typename V>
+__global__ void __launch_bounds__(kThreads, 2) k_persist_batch(const PersistBatchArgs<V> a) {
+    __shared__ State sst;
+    __shared__ int flip;
+    __shared__ unsigned int passed;
+    const int q = a.bprob[blockIdx.x];
+    if (threadIdx.x == 0) {
+        flip = 0;
+        passed = 0u;
+    }
+    {
+        const int n = (int)(sizeof(State) / sizeof(int));
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            reinterpret_cast<int *>(&sst)[k] = reinterpret_cast<const int *>(a.states + q)[k];
+    }
+    __syncthreads();
+    State *st = &sst;
+    const int nb = a.nblk[q], lb = blockIdx.x - a.bfirst[q];
+    const SegPersistB seg{st, a.B.prow[q], a.B.prow[q + 1], lb, nb, a.part + a.poff[q],
+                          a.bars + q, &flip, &passed};
+    auto sync = [&]() -> bool {
+        if (group_sync(a.bars + q, &passed, (unsigned int)nb)) return true;
+        if (threadIdx.x == 0) st->active = 0;
+        __syncthreads();
+        return false;
+    };
+    auto mv = [&](const V *in, V *out, const int *gate2) { d_batch_conn_seg<V>(a.B, seg, in, out, gate2); };
+    const int stop = sst.iter + a.iter_cap;
+    persist_loop<V, SegPersistB>(seg, st, a.v, a.variant, a.jacobi, a.diag, mv, sync, stop);
+    if (lb == 0) {
+        const int n = (int)(sizeof(State) / sizeof(int));
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            reinterpret_cast<int *>(a.states + q)[k] = reinterpret_cast<const int *>(&sst)[k];
     }
 }
 
@@ -1481,12 +1624,100 @@ int run_persist(PH &ph, int variant, cudaStream_t s) {
     return RQ_OK;
 }
 
+// Device areas and the host copy of the row ranges of a persistent batched solve.
+constexpr int kMaxPersistBlocks = 4096;
+constexpr int kPersistIterCap = 256;         // iterations per launch before the blocks re-plan
+constexpr int64_t kPersistRowsPerBlock = 1024;
+struct BatchPersist {
+    const rq_batch_t *b;
+    std::vector<int64_t> prow;  // host copy
+    int32_t *bprob, *bfirst, *nblk;
+    int64_t *poff;
+    GridBar *bars;
+    float4 *part;
+};
+
+// A batched phase as persistent launches: every launch gives each active problem a group of
+// co-resident blocks (one block, plus a share of the rest in proportion to its rows, at most one
+// per kPersistRowsPerBlock rows) and runs up to kPersistIterCap iterations; the host then re-plans
+// over the problems still active, so that the slow problems of the tail get the blocks of those
+// that converged.
+template <typename PH>
+int run_persist_batch(PH &ph, int variant, cudaStream_t s) {
+    using V = typename std::remove_pointer<decltype(ph.v.x)>::type;
+    BatchPersist &bp = *ph.bp;
+    const int P = ph.P;
+    int per = 0;
+    RQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persist_batch<V>, kThreads, 0));
+    int G = per * sm_count();
+    if (G > kMaxPersistBlocks) G = kMaxPersistBlocks;
+    std::vector<State> h(P);
+    std::vector<int32_t> bprob, bfirst(P, 0), nblk(P, 0);
+    std::vector<int64_t> poff(P, 0);
+    std::vector<GridBar> bars(P);
+    while (true) {
+        RQ_CUDA(cudaMemcpyAsync(h.data(), ph.states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
+        RQ_CUDA(cudaStreamSynchronize(s));
+        int64_t rows = 0;
+        int nact = 0;
+        for (int q = 0; q < P; ++q)
+            if (h[q].active) {
+                rows += bp.prow[q + 1] - bp.prow[q];
+                ++nact;
+            }
+        if (nact == 0) break;
+        if (per < 1 || nact > G) {  // more problems than co-resident blocks: CUDA-graph chunks
+            RQ_CUDA(cudaMemcpyAsync(ph.nactive, &nact, sizeof(int), cudaMemcpyHostToDevice, s));
+            RQ_CUDA(cudaStreamSynchronize(s));
+            return run_loop(ph, variant, true, kChunk, s);
+        }
+        const int extra = G - nact;
+        bprob.clear();
+        int64_t pos = 0;
+        for (int q = 0; q < P; ++q) {
+            nblk[q] = 0;
+            bfirst[q] = (int32_t)bprob.size();
+            poff[q] = pos;
+            if (!h[q].active) continue;
+            const int64_t r = bp.prow[q + 1] - bp.prow[q];
+            const int64_t cap = std::max<int64_t>(1, (r + kPersistRowsPerBlock - 1) / kPersistRowsPerBlock);
+            const int64_t n = 1 + (int64_t)((double)extra * (double)r / (double)rows);
+            nblk[q] = (int32_t)std::min(n, cap);
+            for (int k = 0; k < nblk[q]; ++k) bprob.push_back(q);
+            pos += 2 * (int64_t)nblk[q] * kMaxReduce;
+        }
+        const int grid = (int)bprob.size();
+        RQ_CUDA(cudaMemcpyAsync(bp.bprob, bprob.data(), sizeof(int32_t) * grid, cudaMemcpyHostToDevice, s));
+        RQ_CUDA(cudaMemcpyAsync(bp.bfirst, bfirst.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, s));
+        RQ_CUDA(cudaMemcpyAsync(bp.nblk, nblk.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, s));
+        RQ_CUDA(cudaMemcpyAsync(bp.poff, poff.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, s));
+        RQ_CUDA(cudaMemsetAsync(bp.bars, 0, sizeof(GridBar) * P, s));
+        PersistBatchArgs<V> a{ph.states, *bp.b, ph.v, variant, ph.jacobi ? 1 : 0, ph.diag,
+                              kPersistIterCap, bp.bprob, bp.bfirst, bp.nblk, bp.poff, bp.part,
+                              bp.bars};
+        void *args[] = {&a};
+        RQ_CUDA(cudaLaunchCooperativeKernel((const void *)k_persist_batch<V>, dim3(grid),
+                                            dim3(kThreads), args, 0, s));
+        RQ_CUDA(cudaMemcpyAsync(bars.data(), bp.bars, sizeof(GridBar) * P, cudaMemcpyDeviceToHost, s));
+        RQ_CUDA(cudaStreamSynchronize(s));  // (the host vectors above are read by the copies)
+        for (int q = 0; q < P; ++q)
+            if (bars[q].abort) return fail(RQ_E_CUDA, "persistent batched LOBPCG: a barrier timed out");
+    }
+    const int zero = 0;
+    RQ_CUDA(cudaMemcpyAsync(ph.nactive, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+    RQ_CUDA(cudaStreamSynchronize(s));
+    return RQ_OK;
+}
+
 // The iterations of one phase: a persistent kernel when the phase allows it, else CUDA-graph
 // chunks (or eager launches).
 template <typename PH>
 int run_iterations(PH &ph, int variant, bool graph, int chunk, cudaStream_t s) {
     if constexpr (std::is_same<typename std::decay<decltype(ph.seg)>::type, SegOne>::value) {
         if (graph && ph.pop && ph.bar) return run_persist(ph, variant, s);
+    }
+    if constexpr (std::is_same<typename std::decay<decltype(ph.seg)>::type, SegBatch>::value) {
+        if (graph && ph.bp) return run_persist_batch(ph, variant, s);
     }
     return run_loop(ph, variant, graph, chunk, s);
 }
@@ -1816,6 +2047,7 @@ struct BatchPlan {
     std::vector<int32_t> cprob, cofs;
     std::vector<int64_t> crow, cend;
     size_t states, err, part, counter, tcprob, tcrow, tcend, tcofs, vec_hi, vec_lo, total;
+    size_t pb_prob, pb_first, pb_nblk, pb_poff, pb_bars, pb_part;  // persistent launches
     size_t hi_bytes, lo_bytes;
 };
 
@@ -1851,6 +2083,12 @@ int plan_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, BatchPlan &pl) 
     pl.tcrow = take(sizeof(int64_t) * (nch + 1));
     pl.tcend = take(sizeof(int64_t) * nch);
     pl.tcofs = take(sizeof(int32_t) * (P + 1));
+    pl.pb_prob = take(sizeof(int32_t) * kMaxPersistBlocks);
+    pl.pb_first = take(sizeof(int32_t) * P);
+    pl.pb_nblk = take(sizeof(int32_t) * P);
+    pl.pb_poff = take(sizeof(int64_t) * P);
+    pl.pb_bars = take(sizeof(GridBar) * P);
+    pl.pb_part = take(sizeof(float4) * 2 * kMaxPersistBlocks * kMaxReduce);
     pl.hi_bytes = (size_t)b.D * vtype_size(p.vtype);
     pl.lo_bytes = (size_t)b.D * vtype_size(lo_type(p.vtype));
     pl.vec_hi = take(8 * ((pl.hi_bytes + 255) & ~size_t(255)));
@@ -1948,6 +2186,16 @@ int solve_batch(const rq_batch_t &b, const rq_lobpcg_params_t &p, const BatchPla
     BatchBlocks blocks{&pl, P, states, cprob, crow, cend, cofs};
     hi.compact = lo.compact = batch_compact;
     hi.compact_ctx = lo.compact_ctx = &blocks;
+    // cached connectivity: each phase as persistent launches (use_graph 2 keeps the graph chunks;
+    // the Jacobi pass stays on the graph path, as for one problem)
+    BatchPersist bp{&b, pl.prow,
+                    reinterpret_cast<int32_t *>(ws + pl.pb_prob),
+                    reinterpret_cast<int32_t *>(ws + pl.pb_first),
+                    reinterpret_cast<int32_t *>(ws + pl.pb_nblk),
+                    reinterpret_cast<int64_t *>(ws + pl.pb_poff),
+                    reinterpret_cast<GridBar *>(ws + pl.pb_bars),
+                    reinterpret_cast<float4 *>(ws + pl.pb_part)};
+    if (p.use_graph == 1 && b.mode == RQ_MODE_CONN && !jac) hi.bp = lo.bp = &bp;
     std::vector<int> nlo;
     RQ_TRY(run_phases(lo, hi, mixed, p, tol, tol_dim, b.D, x0, pl.hi_bytes, kChunk,
                       p.use_graph != 0, s, nlo));

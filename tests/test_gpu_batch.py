@@ -221,3 +221,28 @@ def test_batch_rejects_wide_problems_and_bad_rows():
     import ctypes
     rc = L.lib().rq_batch_build(ctypes.byref(c), L.ptr(b.scratch), L.stream_ptr())
     assert rc == L.E_ARG
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+@pytest.mark.parametrize('variant', ['reference', 'fast'])
+def test_batch_persistent_launches_match_graph_chunks(variant, precision):
+    """Cached-connectivity batches run each phase as persistent launches (every problem on its own
+    group of blocks, re-planned every 256 iterations); the CUDA-graph chunks run the same
+    iteration: same eigenvalues, iteration counts within one, same eigenvectors."""
+    import torch
+    from rqutils_gb300.batch import BatchedSQD
+    hams, states, ns = _random_problems(31, 40, d_range=(64, 20000))
+    b = BatchedSQD(hams, states, cache_level=(1, 0))
+    rng = np.random.default_rng(32)
+    xr = rng.normal(size=b.D) + 1j * rng.normal(size=b.D)
+    x0 = torch.as_tensor(xr.real if b.is_real else xr).to(b.dtype).cuda()
+    e1, x1, i1 = b.solve(x0=x0, variant=variant, precision=precision, maxiter=3000, use_graph=1)
+    e2, x2, i2 = b.solve(x0=x0, variant=variant, precision=precision, maxiter=3000, use_graph=2)
+    x1, x2 = x1.cpu().numpy(), x2.cpu().numpy()
+    assert max(i['niter'] for i in i1) > 256          # some problem spans several launches
+    for p in range(b.P):
+        assert i1[p]['converged'] == i2[p]['converged'], p
+        assert abs(i1[p]['niter'] - i2[p]['niter']) <= 1, (p, i1[p], i2[p])
+        assert abs(e1[p] - e2[p]) <= 1e-12 * max(1., abs(e2[p])), (p, e1[p], e2[p])
+        r = b.rows(p)
+        assert abs(np.vdot(x1[r], x2[r])) > 1 - 1e-10, p
