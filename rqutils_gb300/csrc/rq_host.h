@@ -70,13 +70,13 @@ struct KernelLaunchCache {
 };
 constexpr int kMaxCachedDevices = 64;
 
-// Opt kern into smem bytes of dynamic shared memory (above the 48 KB default) and return its
-// resident blocks per SM at `block` threads, querying the runtime only when `c` does not hold the
-// answer yet (the occupancy query is also reached while a stream is being captured, where only
-// stream work should be issued).
+// Opt kern into smem bytes of dynamic shared memory (a kernel with static shared memory can need
+// the opt-in below 48 KB of dynamic memory too) and return its resident blocks per SM at `block`
+// threads, querying the runtime only when `c` does not hold the answer yet (the occupancy query
+// is also reached while a stream is being captured, where only stream work should be issued).
 template <typename KernT>
 int configure_kernel(KernT kern, KernelLaunchCache &c, size_t smem, int block, int *per_sm) {
-    if (smem > 48 * 1024 && smem > c.configured) {
+    if (smem > c.configured) {
         RQ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         c.configured = smem;
     }
