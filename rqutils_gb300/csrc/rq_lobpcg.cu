@@ -747,8 +747,52 @@ __global__ void __launch_bounds__(kThreads) k_convert(int64_t D, const VS *a, VD
 
 // Lowest eigenpair of a Hermitian 3x3 given by its strict lower triangle (m10, m20, m21) and its
 // diagonal (complex values, real part used as in ground_locg.py:446); Cardano (Kopp 2008).
+// Smallest root of lambda^3 + c2 lambda^2 + c1 lambda + c0 (three real roots) without FP64
+// transcendental functions: the trigonometric (Cardano) root in FP32 as a seed, then Newton steps
+// on the cubic in FP64 (the reciprocal of f' from an FP32 estimate and one FP64 correction).
+// When the two lowest roots lie within the seed's error Newton may settle on the upper one, so
+// the quotient quadratic lambda^2 + (c2 + x) lambda + c1 + x (c2 + x) gives the other two roots
+// and a smaller one replaces x (random Hermitian 3x3: within 3e-15 of the largest eigenvalue's
+// magnitude; nearly double lowest roots: within 1.6e-8, the FP64 trigonometric formula 2.4e-8).
+// Returns false when the steps do not settle to the FP64 rounding level: the caller then takes
+// the FP64 trigonometric root.
+__device__ __forceinline__ bool cubic_min_root_fast(double c2, double c1, double c0, double p,
+                                                   double q, double disc, double &lam) {
+    // atan2 is scale-free: scale both arguments into FP32 range first
+    const double yd = sqrt(fmax(disc, 0.)), sc = fmax(fabs(yd), fabs(q));
+    if (!(sc > 0.) || !isfinite(sc) || !(p > 0.)) return false;
+    const double isc = 1. / sc;
+    const float phi = atan2f((float)(yd * isc), (float)(q * isc)) * (1.f / 3.f);
+    float cp, sp;
+    sincosf(phi, &sp, &cp);
+    const float s3 = 1.7320508f;
+    const float xmin = fminf(2.f * cp, fminf(-cp - s3 * sp, -cp + s3 * sp));
+    const double sqp = (double)sqrtf((float)p);
+    double x = sqp * (1. / 3.) * (double)xmin - c2 * (1. / 3.);
+    const double tol = 4e-16 * (fabs(x) + sqp);
+    for (int it = 0; it < 4; ++it) {
+        const double f = fma(fma(x + c2, x, c1), x, c0);
+        const double fp = fma(fma(3., x, 2. * c2), x, c1);
+        double r = (double)(1.f / (float)fp);
+        r = r * fma(-fp, r, 2.);  // one Newton step on the reciprocal: ~1e-14 relative
+        const double dx = f * r;
+        x -= dx;
+        if (!isfinite(x)) return false;
+        if (fabs(dx) <= tol) {
+            const double b = c2 + x, c = fma(x, b, c1), d2 = fma(b, b, -4. * c);
+            if (d2 > 0.) {
+                const double rm = (-b - sqrt(d2)) * 0.5;
+                if (rm < x) x = rm;
+            }
+            lam = x;
+            return true;
+        }
+    }
+    return false;
+}
+
 __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2 m11, double2 m22,
-                     double &lam, double2 (&v)[3], bool guard = false) {
+                     double &lam, double2 (&v)[3], bool guard = false, bool fast = false) {
     const double d0 = m00.x, d1 = m11.x, d2 = m22.x;
     const double a10 = m10.x * m10.x + m10.y * m10.y;
     const double a20 = m20.x * m20.x + m20.y * m20.y;
@@ -766,13 +810,16 @@ __device__ void eig3(double2 m10, double2 m20, double2 m21, double2 m00, double2
     // divisions by 3 as products with 1/3 (GB300 runs an FP64 division as a long FP64 sequence
     // on one thread here; the results differ from the quotients by at most an ulp)
     constexpr double kThird = 1. / 3.;
-    const double phi = atan2(sqrt(27. * (0.25 * c1 * c1 * (p - c1) + c0 * (q + 6.75 * c0))), q) * kThird;
-    const double cp = cos(phi), sp = sin(phi), s3 = sqrt(3.);
-    double xmin = 2. * cp;
-    xmin = fmin(xmin, -cp - s3 * sp);
-    xmin = fmin(xmin, -cp + s3 * sp);
-    if (isnan(cp) || isnan(sp)) xmin = NAN;  // jnp.min propagates NaN
-    lam = sqrt(p) * kThird * xmin - c2 * kThird;
+    const double disc = 27. * (0.25 * c1 * c1 * (p - c1) + c0 * (q + 6.75 * c0));
+    if (!(fast && cubic_min_root_fast(c2, c1, c0, p, q, disc, lam))) {
+        const double phi = atan2(sqrt(disc), q) * kThird;
+        const double cp = cos(phi), sp = sin(phi), s3 = sqrt(3.);
+        double xmin = 2. * cp;
+        xmin = fmin(xmin, -cp - s3 * sp);
+        xmin = fmin(xmin, -cp + s3 * sp);
+        if (isnan(cp) || isnan(sp)) xmin = NAN;  // jnp.min propagates NaN
+        lam = sqrt(p) * kThird * xmin - c2 * kThird;
+    }
     // columns 1 and 2 of (A - lambda I): a = (m01, m11 - l, m21), b = (m02, m12, m22 - l)
     const double2 a0 = make_double2(m10.x, -m10.y), a1 = make_double2(m11.x - lam, m11.y), a2 = m21;
     const double2 b0 = m02, b1 = make_double2(m21.x, -m21.y), b2 = make_double2(m22.x - lam, m22.y);
@@ -825,8 +872,9 @@ __device__ __forceinline__ void d_rr3(State *states, int P, int first, int step)
     FOR_ACTIVE_PROBLEMS(states, P, st) {
         double lam;
         double2 v[3];
+        // FAST: the Newton-polished root (no FP64 atan2 / cos / sin on the solve's one thread)
         eig3(st->red[kG10], st->red[kG20], st->red[kG21], st->red[kG00], st->red[kG11],
-             st->red[kG22], lam, v, st->guard != 0);
+             st->red[kG22], lam, v, st->guard != 0, st->variant == RQ_LOBPCG_FAST);
         st->theta = lam;
         for (int k = 0; k < 3; ++k) st->kappa[k] = v[k];
         break;
