@@ -81,13 +81,20 @@ class BatchedSQD:
     """
 
     def __init__(self, hamiltonians, states_list, cache_level=(0, 0), states_sizes=None,
-                 filter=True, device=None, stream=None, presence=None):
+                 filter=True, device=None, stream=None, presence=None, tune_cache=None):
+        """``cache_level='auto'``: matrix-free or cached connectivity, chosen by measurement
+        (``rqutils_gb300.autotune.tune_batch``, recorded per problem class in ``tune_cache``)."""
         if len(hamiltonians) != len(states_list) or not hamiltonians:
             raise ValueError('need one subspace per Hamiltonian and at least one problem')
         self.device = device or default_device()
         hams = [h if isinstance(h, PauliSumXZ)
                 else PauliSumXZ.from_paulisum(h, force_real=True, add_padding=True)
                 for h in hamiltonians]
+        if cache_level == 'auto':
+            from .autotune import tune_batch
+            sl = [subspace_states(s, h.num_qubits) for h, s in zip(hams, states_list)]
+            mode, _ = tune_batch(hams, sl, cache=tune_cache, device=self.device)
+            cache_level = (0, 0) if mode == 'free' else (1, 0)
         for h in hams:
             if h.num_qubits > STATE_BITS:
                 raise ValueError(f'batched problems have at most {STATE_BITS} qubits')

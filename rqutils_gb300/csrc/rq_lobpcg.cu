@@ -1245,10 +1245,11 @@ int read_active(const int *nactive, int &h, cudaStream_t s) {
     return RQ_OK;
 }
 
-// Run iterations until no problem is active.  With use_graph the chunk is captured once and
-// relaunched; otherwise launched eagerly.  Callbacks run one iteration per chunk.
+// Run iterations until no problem is active (or no more than stop_below).  With use_graph the
+// chunk is captured once and relaunched; otherwise launched eagerly.  Callbacks run one iteration
+// per chunk.
 template <typename PH>
-int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s) {
+int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s, int stop_below = 0) {
     int active = 0;
     auto enqueue_chunk = [&](cudaStream_t cs) -> int {
         for (int k = 0; k < chunk; ++k) RQ_TRY(ph.iteration(variant, cs));
@@ -1258,7 +1259,7 @@ int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s) {
         while (true) {
             RQ_TRY(enqueue_chunk(s));
             RQ_TRY(read_active(ph.nactive, active, s));
-            if (active <= 0) break;
+            if (active <= stop_below) break;
         }
         return RQ_OK;
     }
@@ -1286,7 +1287,7 @@ int run_loop(PH &ph, int variant, bool use_graph, int chunk, cudaStream_t s) {
         e = cudaGraphLaunch(exec, s);
         if (e != cudaSuccess) break;
         rc = read_active(ph.nactive, active, s);
-        if (rc != RQ_OK || active <= 0) break;
+        if (rc != RQ_OK || active <= stop_below) break;
         if (ph.compact && active * 4 <= last) {
             // most problems have converged: launch blocks for the remaining ones only
             cudaGraphExecDestroy(exec);
@@ -1685,11 +1686,13 @@ struct BatchPersist {
     float4 *part;
 };
 
-// A batched phase as persistent launches: every launch gives each active problem a group of
-// co-resident blocks (one block, plus a share of the rest in proportion to its rows, at most one
-// per kPersistRowsPerBlock rows) and runs up to kPersistIterCap iterations; the host then re-plans
-// over the problems still active, so that the slow problems of the tail get the blocks of those
-// that converged.
+// A batched phase with persistent launches for its tail.  While more problems are active than a
+// quarter of the co-resident blocks, CUDA-graph chunks run them (blocks of 2048 rows: every row of
+// every problem gets a thread group, however many problems there are).  Then every launch gives
+// each remaining problem a group of co-resident blocks (one block, plus a share of the rest in
+// proportion to its rows, at most one per kPersistRowsPerBlock rows) and runs up to
+// kPersistIterCap iterations; the host re-plans over the problems still active, so that the slow
+// problems of the tail get the blocks of those that converged.
 template <typename PH>
 int run_persist_batch(PH &ph, int variant, cudaStream_t s) {
     using V = typename std::remove_pointer<decltype(ph.v.x)>::type;
@@ -1714,10 +1717,12 @@ int run_persist_batch(PH &ph, int variant, cudaStream_t s) {
                 ++nact;
             }
         if (nact == 0) break;
-        if (per < 1 || nact > G) {  // more problems than co-resident blocks: CUDA-graph chunks
+        if (per < 1) return run_loop(ph, variant, true, kChunk, s);
+        if (nact > G / 4) {  // many problems: graph chunks until a quarter of G remain
             RQ_CUDA(cudaMemcpyAsync(ph.nactive, &nact, sizeof(int), cudaMemcpyHostToDevice, s));
             RQ_CUDA(cudaStreamSynchronize(s));
-            return run_loop(ph, variant, true, kChunk, s);
+            RQ_TRY(run_loop(ph, variant, true, kChunk, s, G / 4));
+            continue;
         }
         const int extra = G - nact;
         bprob.clear();

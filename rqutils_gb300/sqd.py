@@ -129,14 +129,31 @@ class SQDProblem:
     """Hamiltonian terms and subspace on the device with the operator built for cache_level."""
 
     def __init__(self, hamiltonian, states_u64, cache_level=(1, 0), lookup='hash',
-                 filter_masks=None, device=None, precision='fp64'):
+                 filter_masks=None, device=None, precision='fp64', line_bits=8, tune_cache=None):
+        """``cache_level='auto'``: the form of the product (matrix-free with or without the line
+        filter, binary search, cached connectivity or elements) is chosen by measurement
+        (``rqutils_gb300.autotune.tune``, recorded per problem class in ``tune_cache``)."""
         self.device = device or default_device()
         self.ham = hamiltonian
         self.n = hamiltonian.num_qubits
         self.states = states_u64
+        line_filter = True
+        if cache_level == 'auto':
+            from .autotune import tune
+            single = precision == 'fp32'
+            if hamiltonian.is_real:
+                dt = torch.float32 if single else torch.float64
+            else:
+                dt = torch.complex64 if single else torch.complex128
+            (mode, lookup, lb), _ = tune(hamiltonian, states_u64, dtype=dt, cache=tune_cache,
+                                         device=self.device)
+            line_filter, line_bits = lb > 0, lb or 8
+            cache_level = {'free': (0, 0), 'conn': (1, 0), 'csr': (1, 2)}[mode]
+        self.cache_level = cache_level
         self.terms = DeviceTerms(hamiltonian, device=self.device)
         self.sub = DeviceSubspace(states_u64, num_qubits=self.n, lookup=lookup,
-                                  filter_masks=filter_masks, device=self.device)
+                                  filter_masks=filter_masks, device=self.device,
+                                  line_filter=line_filter, line_bits=line_bits)
         mode = cache_mode(cache_level)
         csr_vtype = None
         if mode == 'csr':
@@ -161,6 +178,9 @@ def sqd(hamiltonian, states, states_size=None, return_eigvec=True, cache_level=(
         precision='fp64', variant='reference', lookup='hash', maxiter=1000, tol=None,
         target_rel=None, jacobi=False, use_graph=True, return_info=False, device=None):
     """Ground eigenpair of the Hamiltonian projected on the subspace spanned by ``states``.
+
+    ``cache_level`` is the reference's (0, *), (1, 0|1) or (*, 2), or ``'auto'`` (not in the
+    reference): the form of the product chosen by measurement (``rqutils_gb300.autotune``).
 
     Returns the energy, or ``(energy, eigvec (D,), basis_states (D, n) uint8)`` with
     ``return_eigvec`` (sqd.py:243-248); ``return_info`` appends a dict of solver statistics.

@@ -243,6 +243,9 @@ def test_batch_persistent_launches_match_graph_chunks(variant, precision):
     for p in range(b.P):
         assert i1[p]['converged'] == i2[p]['converged'], p
         assert abs(i1[p]['niter'] - i2[p]['niter']) <= 1, (p, i1[p], i2[p])
+        if np.isnan(e2[p]):  # the same breakdown on both paths
+            assert np.isnan(e1[p]), p
+            continue
         assert abs(e1[p] - e2[p]) <= 1e-12 * max(1., abs(e2[p])), (p, e1[p], e2[p])
         r = b.rows(p)
         assert abs(np.vdot(x1[r], x2[r])) > 1 - 1e-10, p
