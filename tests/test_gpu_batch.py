@@ -228,7 +228,9 @@ def test_batch_rejects_wide_problems_and_bad_rows():
 def test_batch_persistent_launches_match_graph_chunks(variant, precision):
     """Cached-connectivity batches run each phase as persistent launches (every problem on its own
     group of blocks, re-planned every 256 iterations); the CUDA-graph chunks run the same
-    iteration: same eigenvalues, iteration counts within one, same eigenvectors."""
+    iteration: same eigenvalues and eigenvectors, iteration counts within one in FP64.  With a
+    32-bit phase the two block layouts add the FP32 partial sums in different orders, which can
+    move the switch to FP64 by some iterations (10 % here)."""
     import torch
     from rqutils_gb300.batch import BatchedSQD
     hams, states, ns = _random_problems(31, 40, d_range=(64, 20000))
@@ -242,7 +244,8 @@ def test_batch_persistent_launches_match_graph_chunks(variant, precision):
     assert max(i['niter'] for i in i1) > 256          # some problem spans several launches
     for p in range(b.P):
         assert i1[p]['converged'] == i2[p]['converged'], p
-        assert abs(i1[p]['niter'] - i2[p]['niter']) <= 1, (p, i1[p], i2[p])
+        slack = 1 if precision == 'fp64' else max(2, int(0.1 * i2[p]['niter']))
+        assert abs(i1[p]['niter'] - i2[p]['niter']) <= slack, (p, i1[p], i2[p])
         if np.isnan(e2[p]):  # the same breakdown on both paths
             assert np.isnan(e1[p]), p
             continue
