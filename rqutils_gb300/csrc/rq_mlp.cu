@@ -481,13 +481,39 @@ __global__ void __launch_bounds__(kHid) k_head_bwd(const bf16 *__restrict__ z2, 
     }
 }
 
-// dst[c] = sum_t part[t * ncols + c] in t order
-__global__ void k_colsum(const float *__restrict__ part, int64_t nt, int64_t ncols, float *__restrict__ dst) {
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncols; c += (int64_t)gridDim.x * blockDim.x) {
+// dst[c] = sum_t part[t * ncols + c]: a block of kColsumWarps warps per 32 columns (lane =
+// column: every row of partials is read coalesced); warp w adds the rows t in its contiguous
+// range with four interleaved accumulators, then warp 0 adds the warp sums in warp order.  The
+// order of every addition is fixed, so the sums are the same on every run.
+constexpr int kColsumWarps = 32;
+__global__ void __launch_bounds__(kColsumWarps * 32)
+k_colsum(const float *__restrict__ part, int64_t nt, int64_t ncols, float *__restrict__ dst) {
+    __shared__ float ws[kColsumWarps][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t c = (int64_t)blockIdx.x * 32 + lane;
+    const int64_t t0 = w * nt / kColsumWarps, t1 = (w + 1) * nt / kColsumWarps;
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    if (c < ncols) {
+        int64_t t = t0;
+        for (; t + 4 <= t1; t += 4) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) a[k] += __ldg(part + (t + k) * ncols + c);
+        }
+        for (int k = 0; t < t1; ++t, ++k) a[k] += __ldg(part + t * ncols + c);
+    }
+    ws[w][lane] = (a[0] + a[1]) + (a[2] + a[3]);
+    __syncthreads();
+    if (w == 0 && c < ncols) {
         float s = 0.f;
-        for (int64_t t = 0; t < nt; ++t) s += part[t * ncols + c];
+        for (int k = 0; k < kColsumWarps; ++k) s += ws[k][lane];
         dst[c] = s;
     }
+}
+
+int launch_colsum(const float *part, int64_t nt, int64_t ncols, float *dst, cudaStream_t st) {
+    k_colsum<<<(unsigned)((ncols + 31) / 32), kColsumWarps * 32, 0, st>>>(part, nt, ncols, dst);
+    RQ_CUDA(cudaGetLastError());
+    return RQ_OK;
 }
 
 __device__ __forceinline__ void write_bf16_copies(const rq_mlp_t &M, int i, float p) {
@@ -720,14 +746,13 @@ RQ_API int rq_mlp_bwd(const rq_mlp_t *m, int64_t rows, const uint16_t *xt, const
     b.out = reinterpret_cast<float *>(w + L.split1);
     b.err = err;
     RQ_TRY((launch_gemm<kIn, EPI_F32>(b, kHid / kTileM, L.nsplit, st)));
-    k_colsum<<<grid_for(kHid * kIn), kThreads, 0, st>>>(reinterpret_cast<const float *>(w + L.split1), L.nsplit,
-                                                       kHid * kIn, m->grads + kOffW1);
-    k_colsum<<<grid_for(kHid), kThreads, 0, st>>>(reinterpret_cast<const float *>(w + L.colpart1), L.tiles, kHid,
-                                                 m->grads + kOffB1);
-    k_colsum<<<grid_for(kHid * kHid), kThreads, 0, st>>>(reinterpret_cast<const float *>(w + L.split2), L.nsplit,
-                                                        kHid * kHid, m->grads + kOffW2);
-    k_colsum<<<grid_for(kHeadPart), kThreads, 0, st>>>(part2, L.tiles, kHeadPart, m->grads + kOffB2);
-    RQ_CUDA(cudaGetLastError());
+    RQ_TRY(launch_colsum(reinterpret_cast<const float *>(w + L.split1), L.nsplit, kHid * kIn,
+                         m->grads + kOffW1, st));
+    RQ_TRY(launch_colsum(reinterpret_cast<const float *>(w + L.colpart1), L.tiles, kHid,
+                         m->grads + kOffB1, st));
+    RQ_TRY(launch_colsum(reinterpret_cast<const float *>(w + L.split2), L.nsplit, kHid * kHid,
+                         m->grads + kOffW2, st));
+    RQ_TRY(launch_colsum(part2, L.tiles, kHeadPart, m->grads + kOffB2, st));
     return RQ_OK;
 }
 
