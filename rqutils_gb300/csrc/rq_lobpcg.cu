@@ -1228,15 +1228,6 @@ struct Phase {
         RQ_CUDA(cudaGetLastError());
         return RQ_OK;
     }
-
-    // continuation from x, y of another phase (already converted into v.x, v.y): fresh A x, r
-    int resume(int variant, cudaStream_t s) {
-        RQ_TRY(matvec(v.x, v.ax, s));
-        if (variant == RQ_LOBPCG_FAST) RQ_TRY(matvec(v.y, v.ay, s));
-        k_resid<V, SEG><<<grid, kThreads, 0, s>>>(seg, v.ax, v.x, v.r, 0);
-        RQ_CUDA(cudaGetLastError());
-        return RQ_OK;
-    }
 };
 
 int read_active(const int *nactive, int &h, cudaStream_t s) {
@@ -1835,17 +1826,13 @@ int run_phases(PLO &lo, PHI &hi, bool mixed, const rq_lobpcg_params_t &p, double
         RQ_CUDA(cudaMemcpyAsync(h.data(), lo.states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
         RQ_CUDA(cudaStreamSynchronize(s));
         for (int q = 0; q < P; ++q) niter_lo[q] = h[q].iter;
-        // continue in the final type from x and y, each problem with its own theta
+        // restart in the final type from x alone: the 32-bit phase's search direction y is mostly
+        // rounding noise once the residual nears the 32-bit floor, and a three-term step that
+        // carries it on converges at the rate of steepest descent (thousands of iterations where
+        // a restart from x takes a few hundred)
         k_convert<VLO, VHI><<<gconv, kThreads, 0, s>>>(D, lo.v.x, hi.v.x);
-        k_convert<VLO, VHI><<<gconv, kThreads, 0, s>>>(D, lo.v.y, hi.v.y);
         RQ_TRY(init_states(hi.states, hi.nactive, P, p, tol, tol_dim, false, s));
-        std::vector<State> h2(P);
-        RQ_CUDA(cudaMemcpyAsync(h2.data(), hi.states, sizeof(State) * P, cudaMemcpyDeviceToHost, s));
-        RQ_CUDA(cudaStreamSynchronize(s));
-        for (int q = 0; q < P; ++q) h2[q].theta = h[q].theta;
-        RQ_CUDA(cudaMemcpyAsync(hi.states, h2.data(), sizeof(State) * P, cudaMemcpyHostToDevice, s));
-        RQ_TRY(hi.resume(p.variant, s));
-        RQ_CUDA(cudaStreamSynchronize(s));  // h2 is a stack vector
+        RQ_TRY(hi.start(p.variant, s));
     } else {
         RQ_TRY(init_states(hi.states, hi.nactive, P, p, tol, tol_dim, false, s));
         RQ_CUDA(cudaMemcpyAsync(hi.v.x, x0, hi_bytes, cudaMemcpyDeviceToDevice, s));

@@ -230,7 +230,8 @@ def test_batch_persistent_launches_match_graph_chunks(variant, precision):
     group of blocks, re-planned every 256 iterations); the CUDA-graph chunks run the same
     iteration: same eigenvalues and eigenvectors, iteration counts within one in FP64.  With a
     32-bit phase the two block layouts add the FP32 partial sums in different orders, which can
-    move the switch to FP64 by some iterations (10 % here)."""
+    move the switch to FP64 by some iterations (10 % here) and the final vectors within the
+    residual test."""
     import torch
     from rqutils_gb300.batch import BatchedSQD
     hams, states, ns = _random_problems(31, 40, d_range=(64, 20000))
@@ -251,4 +252,5 @@ def test_batch_persistent_launches_match_graph_chunks(variant, precision):
             continue
         assert abs(e1[p] - e2[p]) <= 1e-12 * max(1., abs(e2[p])), (p, e1[p], e2[p])
         r = b.rows(p)
-        assert abs(np.vdot(x1[r], x2[r])) > 1 - 1e-10, p
+        # both vectors meet the residual test, so they agree to about (residual / gap)^2
+        assert abs(np.vdot(x1[r], x2[r])) > 1 - (1e-10 if precision == 'fp64' else 1e-8), p
