@@ -724,8 +724,17 @@ def run_profile(args):
         t0 = time.perf_counter()
         m.fit(S, np.linspace(2, 8, 8), psi, steps=args.steps, batch=65536)
         torch.cuda.synchronize()
-        print(json.dumps({'profile_steps': args.steps,
-                          'ms_per_step': 1e3 * (time.perf_counter() - t0) / args.steps}), flush=True)
+        ms = 1e3 * (time.perf_counter() - t0) / args.steps
+        # then inference over 2^18 states (the warm-start evaluation's subspace size)
+        S2 = torch.as_tensor(np.sort(rng.choice(1 << 32, size=1 << 18, replace=False)).view(np.int64),
+                             device=dev)
+        m.predict(S2, 5.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.predict(S2, 5.0)
+        torch.cuda.synchronize()
+        print(json.dumps({'profile_steps': args.steps, 'ms_per_step': ms,
+                          'predict_2^18_ms': 1e3 * (time.perf_counter() - t0)}), flush=True)
         return
     wl = Workload(args.workload, args.rows)
     terms = DeviceTerms(wl.ham, device=dev)

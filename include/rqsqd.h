@@ -326,6 +326,13 @@ typedef struct rq_batch {
     const int64_t *states_size; /* [P] HOST array: each problem's convergence length (sqd's
                                    states_size, sqd.py:222-225); NULL = its row count        */
     uint32_t *pmap;            /* [2^pbits / 32] presence bitmap over the composite keys       */
+    uint32_t *lmap;            /* line filter over the composite keys (as rq_subspace_t.lmap, with
+                                  each problem's own prefix shift), or NULL; replaces pmap     */
+    uint32_t *xline;           /* [J] written by rq_batch_build: hash(xmask >> shift of the
+                                  group's problem)                                           */
+    int32_t  *lshift;          /* [P] written by rq_batch_build: each problem's prefix shift    */
+    int32_t   lbits;           /* rq_line_filter_bits(D, lwbits, &lbits)                         */
+    int32_t   lwbits;          /* 8 .. 10                                                        */
 } rq_batch_t;
 
 /* Validate the keys, fill the hash table, the per-problem sector filters and diag0.
@@ -389,6 +396,10 @@ int rq_mlp_sample(const uint64_t *states, int64_t D, const double *U, const floa
 /* out[rows][2] = f(x); keeps the activations in ws for rq_mlp_bwd. */
 int rq_mlp_fwd(const rq_mlp_t *m, int64_t rows, const uint16_t *x, float *out, void *ws,
                void *stream);
+/* out[rows][2] = f(x) without keeping the activations for rq_mlp_bwd (inference: only the
+ * hidden activations that layer 2 reads are written to ws). */
+int rq_mlp_infer(const rq_mlp_t *m, int64_t rows, const uint16_t *x, float *out, void *ws,
+                 void *stream);
 /* dout[rows][2] of the weighted loss mean_i w_i ((o0 - a_i)^2 + softplus(-s_i o1)); the loss
  * itself is written to loss[0] (device double) when loss is not NULL. */
 int rq_mlp_loss(int64_t rows, const float *out, const float *tgt, float *dout, double *loss,
@@ -396,6 +407,14 @@ int rq_mlp_loss(int64_t rows, const float *out, const float *tgt, float *dout, d
 /* m->grads = d loss / d params from dout and the activations of the last rq_mlp_fwd on ws. */
 int rq_mlp_bwd(const rq_mlp_t *m, int64_t rows, const uint16_t *xt, const float *dout, void *ws,
                void *stream);
+/* One training step without the Adam update: forward, loss and backward of a minibatch (rows a
+ * multiple of 128; x[rows][64] and xt[64][rows] BF16, tgt[rows][3] as rq_mlp_sample writes them).
+ * m->grads = d loss / d params; out[rows][2] = f(x) when out is not NULL; loss[0] (device double)
+ * = the loss of rq_mlp_loss when loss is not NULL.  Layer 2's epilogue computes the loss gradient
+ * and dZ2 in place (the same gradients as rq_mlp_fwd + rq_mlp_loss + rq_mlp_bwd, with Z2 kept in
+ * FP32 rather than rounded to BF16). */
+int rq_mlp_train(const rq_mlp_t *m, int64_t rows, const uint16_t *x, const uint16_t *xt,
+                 const float *tgt, float *out, double *loss, void *ws, void *stream);
 /* One Adam step (step number t >= 1) on params from grads; refreshes the BF16 copies. */
 int rq_mlp_step(const rq_mlp_t *m, int32_t t, float lr, float beta1, float beta2, float eps,
                 void *stream);

@@ -68,7 +68,9 @@ class Batch(ctypes.Structure):
                 ('empty_key', ctypes.c_uint64), ('fmask', _c_void_p), ('fbits', _c_void_p),
                 ('terms', Terms), ('gofs', _c_void_p), ('dgrp', _c_void_p), ('diag0', _c_void_p),
                 ('rowptr', _c_void_p), ('col', _c_void_p), ('grp', _c_void_p),
-                ('nnz', ctypes.c_int64), ('states_size', _c_void_p), ('pmap', _c_void_p)]
+                ('nnz', ctypes.c_int64), ('states_size', _c_void_p), ('pmap', _c_void_p),
+                ('lmap', _c_void_p), ('xline', _c_void_p), ('lshift', _c_void_p),
+                ('lbits', ctypes.c_int32), ('lwbits', ctypes.c_int32)]
 
 
 BATCH_STATE_BITS = 40
@@ -139,10 +141,14 @@ SIGNATURES = {
                                      ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
     'rq_mlp_fwd': (ctypes.c_int, [_P(Mlp), ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
                                   _c_void_p]),
+    'rq_mlp_infer': (ctypes.c_int, [_P(Mlp), ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
+                                    _c_void_p]),
     'rq_mlp_loss': (ctypes.c_int, [ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
                                    _c_void_p, _c_void_p]),
     'rq_mlp_bwd': (ctypes.c_int, [_P(Mlp), ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
                                   _c_void_p]),
+    'rq_mlp_train': (ctypes.c_int, [_P(Mlp), ctypes.c_int64, _c_void_p, _c_void_p, _c_void_p,
+                                    _c_void_p, _c_void_p, _c_void_p, _c_void_p]),
     'rq_mlp_step': (ctypes.c_int, [_P(Mlp), ctypes.c_int32, ctypes.c_float, ctypes.c_float,
                                    ctypes.c_float, ctypes.c_float, _c_void_p]),
     'rq_mlp_warm_start': (ctypes.c_int, [ctypes.c_int64, _c_void_p, ctypes.c_int32, _c_void_p,

@@ -81,9 +81,13 @@ class BatchedSQD:
     """
 
     def __init__(self, hamiltonians, states_list, cache_level=(0, 0), states_sizes=None,
-                 filter=True, device=None, stream=None, presence=None, tune_cache=None):
+                 filter=True, device=None, stream=None, presence=None, tune_cache=None,
+                 line_filter=True, line_bits=8):
         """``cache_level='auto'``: matrix-free or cached connectivity, chosen by measurement
-        (``rqutils_gb300.autotune.tune_batch``, recorded per problem class in ``tune_cache``)."""
+        (``rqutils_gb300.autotune.tune_batch``, recorded per problem class in ``tune_cache``).
+        ``line_filter``: probe a line filter over the composite keys (2^line_bits-bit lines, each
+        problem with its own prefix shift) before the hash table; it replaces the presence
+        bitmap (``presence``), which is used only without it."""
         if len(hamiltonians) != len(states_list) or not hamiltonians:
             raise ValueError('need one subspace per Hamiltonian and at least one problem')
         self.device = device or default_device()
@@ -145,6 +149,19 @@ class BatchedSQD:
         pb = ctypes.c_int32()
         L.check(lib.rq_presence_bits(self.D, 64, ctypes.byref(pb)), 'rq_presence_bits')
         self.pbits = pb.value if presence is None else (0 if presence is False else int(presence))
+        if line_filter:
+            self.pbits = 0
+            lb = ctypes.c_int32()
+            L.check(lib.rq_line_filter_bits(self.D, int(line_bits), ctypes.byref(lb)),
+                    'rq_line_filter_bits')
+            self.lbits, self.lwbits = lb.value, int(line_bits)
+            self.lmap = torch.empty(1 << (self.lbits + self.lwbits - 5), dtype=torch.int32,
+                                    device=dev)
+            self.xline = torch.empty(max(J, 1), dtype=torch.int32, device=dev)
+            self.lshift = torch.empty(self.P, dtype=torch.int32, device=dev)
+        else:
+            self.lbits = self.lwbits = 0
+            self.lmap = self.xline = self.lshift = None
         self.pmap = (torch.empty((1 << self.pbits) // 32, dtype=torch.int32, device=dev)
                      if self.pbits else None)
         if filter:
@@ -162,7 +179,8 @@ class BatchedSQD:
                          fmask=L.ptr(self.fmask), fbits=L.ptr(self.fbits), terms=terms,
                          gofs=L.ptr(self.gofs), dgrp=L.ptr(self.dgrp), diag0=L.ptr(self.diag0),
                          states_size=ctypes.cast(self.states_size, ctypes.c_void_p),
-                         pmap=L.ptr(self.pmap))
+                         pmap=L.ptr(self.pmap), lmap=L.ptr(self.lmap), xline=L.ptr(self.xline),
+                         lshift=L.ptr(self.lshift), lbits=self.lbits, lwbits=self.lwbits)
         L.check(lib.rq_batch_build(ctypes.byref(self.c), L.ptr(self.scratch), L.stream_ptr(stream)),
                 'rq_batch_build')
         self.rowptr = self.col = self.grp = None

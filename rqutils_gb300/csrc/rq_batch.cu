@@ -100,6 +100,60 @@ __device__ __forceinline__ cx<R> bgroup_diag(const rq_terms_t &T, int g, uint64_
     return d.get();
 }
 
+// Line filter of a batch, per problem p (block p): the prefix shift lshift[p] from the highest
+// differing bit of the problem's neighbouring keys (the largest shift with about 2^(lwbits - 5)
+// keys per distinct prefix, as for one subspace), then xline[g] = hash(xmask[g] >> lshift[p]) for
+// the problem's groups.
+__global__ void __launch_bounds__(kThreads)
+k_batch_line_prep(const uint64_t *__restrict__ keys, const int64_t *__restrict__ prow,
+                  const uint64_t *__restrict__ xmask, const int32_t *__restrict__ gofs, int lwbits,
+                  int32_t *__restrict__ lshift, uint32_t *__restrict__ xline) {
+    __shared__ uint32_t T[kHashTableWords];
+    __shared__ unsigned int hist[64];
+    __shared__ int shift_s;
+    const int p = blockIdx.x;
+    init_hash_tables(T, 8);
+    if (threadIdx.x < 64) hist[threadIdx.x] = 0u;
+    __syncthreads();
+    const int64_t r0 = prow[p], r1 = prow[p + 1];
+    for (int64_t i = r0 + 1 + threadIdx.x; i < r1; i += blockDim.x)
+        atomicAdd(&hist[63 - __clzll((long long)(keys[i] ^ keys[i - 1]))], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double per = (double)(1 << (lwbits - 5));
+        const double Dp = (double)(r1 - r0);
+        unsigned long long above = 0;  // distinct prefixes at shift b, minus one
+        for (int k = 0; k < 64; ++k) above += hist[k];
+        int b = 0;
+        for (int c = 1; c <= kStateBits; ++c) {
+            above -= hist[c - 1];
+            if (Dp > per * (double)(above + 1)) break;
+            b = c;
+        }
+        shift_s = b;
+        lshift[p] = b;
+    }
+    __syncthreads();
+    const int b = shift_s;
+    for (int g = gofs[p] + threadIdx.x; g < gofs[p + 1]; g += blockDim.x) xline[g] = lin_hash(T, xmask[g] >> b, 8);
+}
+
+// bit (hash(key) mod 2^lwbits) of line hash(key >> lshift[p]) >> (32 - lbits) for every key
+__global__ void __launch_bounds__(kThreads)
+k_batch_line_build(const uint64_t *__restrict__ keys, int64_t D, const int32_t *__restrict__ lshift,
+                   uint32_t *__restrict__ lmap, int lbits, int lwbits) {
+    __shared__ uint32_t T[kHashTableWords];
+    init_hash_tables(T, 8);
+    __syncthreads();
+    const uint32_t bmask = (1u << lwbits) - 1u;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        const uint32_t line = lin_hash(T, k >> lshift[problem_of(k)], 8) >> (32 - lbits);
+        const uint32_t bit = lin_hash(T, k, 8) & bmask;
+        atomicOr(lmap + ((size_t)line << (lwbits - 5)) + (bit >> 5), 1u << (bit & 31));
+    }
+}
+
 __device__ __forceinline__ bool gate_open(const int *gate, int64_t stride, const int *gate2, int p) {
     if (!gate) return true;
     if (!*reinterpret_cast<const int *>(reinterpret_cast<const char *>(gate) + p * stride))
@@ -132,6 +186,11 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
     const unsigned char *keys = static_cast<const unsigned char *>(B.hkeys);
     const uint64_t *xm = B.terms.xmask + g0;
     const uint32_t *xh = B.terms.xhash + g0;
+    const uint32_t *xl = B.lmap ? B.xline + g0 : nullptr;
+    // line filter: the row's prefix hash once; a target's line is (hls ^ xline[g]) >> lsh
+    const uint32_t hls = (B.lmap && act) ? lin_hash(htab, key >> B.lshift[p], 8) : 0u;
+    const int lsh = 32 - B.lbits, lwsh = B.lwbits - 5;
+    const uint32_t lbmask = (1u << B.lwbits) - 1u;
     constexpr int U = 4;
     for (int r0 = 0; r0 < nmax; r0 += 64) {
         const int r1 = min(ng, r0 + 64);
@@ -174,7 +233,16 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
                 t[u] = key ^ xv;
                 b[u] = hs ^ hx;
             }
-            if (B.pbits > 0) {
+            if (xl) {
+                uint32_t lw[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t ln = q[u] ? (hls ^ __ldg(xl + r0 + rr[u])) >> lsh : 0u;
+                    lw[u] = q[u] ? __ldg(B.lmap + ((size_t)ln << lwsh) + ((b[u] & lbmask) >> 5)) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) q[u] = q[u] && ((lw[u] >> (b[u] & 31)) & 1u);
+            } else if (B.pbits > 0) {
                 uint32_t pw[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
@@ -369,6 +437,8 @@ RQ_API int rq_batch_build(rq_batch_t *b, void *scratch, void *stream) {
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
     if (b->pbits != 0 && (!b->pmap || b->pbits < 5 || b->pbits > 32 || b->pbits < b->hbits))
         return fail(RQ_E_ARG, "rq_batch_build: presence bitmap missing or pbits out of range");
+    if (b->lmap && (!b->xline || !b->lshift || b->lbits < 1 || b->lbits > 31 || b->lwbits < 8 || b->lwbits > 10))
+        return fail(RQ_E_ARG, "rq_batch_build: line filter needs xline, lshift, 1 <= lbits <= 31, 8 <= lwbits <= 10");
     int rc = build_key_table(b->keys, b->D, 64, true, b->hkeys, b->hvals, b->hbits, &b->empty_key,
                              flag, gap, st, b->pbits ? b->pmap : nullptr, b->pbits);
     if (rc != RQ_OK) return fail(rc, std::string("rq_batch_build: ") + rq_last_error());
@@ -385,6 +455,13 @@ RQ_API int rq_batch_build(rq_batch_t *b, void *scratch, void *stream) {
         k_fill_all_bits<<<grid_rows(nwords), kThreads, 0, st>>>(b->fbits, nwords);
     }
     k_batch_diag<<<grid_rows(b->D), kThreads, 0, st>>>(b->keys, b->D, b->dgrp, b->terms, b->diag0);
+    if (b->lmap) {
+        k_batch_line_prep<<<b->P, kThreads, 0, st>>>(b->keys, b->prow, b->terms.xmask, b->gofs, b->lwbits,
+                                                      b->lshift, b->xline);
+        RQ_CUDA(cudaMemsetAsync(b->lmap, 0, (size_t)1 << (b->lbits + b->lwbits - 3), st));
+        k_batch_line_build<<<grid_rows(b->D), kThreads, 0, st>>>(b->keys, b->D, b->lshift, b->lmap, b->lbits,
+                                                                  b->lwbits);
+    }
     RQ_CUDA(cudaGetLastError());
     int h_flag = 0;
     RQ_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));

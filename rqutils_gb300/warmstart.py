@@ -84,6 +84,16 @@ class WarmStartMLP:
                                    L.stream_ptr(stream)), 'rq_mlp_fwd')
         return out
 
+    def infer(self, x, out=None, stream=None):
+        """out (rows, 2) FP32 for BF16 features x (rows, 64), keeping no activations."""
+        rows = x.shape[0]
+        ws = self.workspace(rows)
+        if out is None:
+            out = torch.empty((rows, 2), dtype=torch.float32, device=self.device)
+        L.check(L.lib().rq_mlp_infer(ctypes.byref(self.c), rows, L.ptr(x), L.ptr(out), L.ptr(ws),
+                                     L.stream_ptr(stream)), 'rq_mlp_infer')
+        return out
+
     def loss(self, out, tgt, dout=None, loss=None, stream=None):
         rows = out.shape[0]
         ws = self.workspace(rows)
@@ -99,6 +109,17 @@ class WarmStartMLP:
         ws = self.workspace(rows)
         L.check(L.lib().rq_mlp_bwd(ctypes.byref(self.c), rows, L.ptr(xt), L.ptr(dout), L.ptr(ws),
                                    L.stream_ptr(stream)), 'rq_mlp_bwd')
+        return self.grads
+
+    def train_step(self, x, xt, tgt, out=None, loss=None, stream=None):
+        """Forward, loss and backward of one minibatch in one call (rq_mlp_train): grads from
+        features x (rows, 64), their transpose xt (64, rows) and targets tgt (rows, 3).  The
+        loss (device double, shape (1,)) is written when ``loss`` is given."""
+        rows = x.shape[0]
+        ws = self.workspace(rows)
+        L.check(L.lib().rq_mlp_train(ctypes.byref(self.c), rows, L.ptr(x), L.ptr(xt), L.ptr(tgt),
+                                     L.ptr(out), L.ptr(loss), L.ptr(ws), L.stream_ptr(stream)),
+                'rq_mlp_train')
         return self.grads
 
     def step(self, lr, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
@@ -126,8 +147,6 @@ class WarmStartMLP:
         x = torch.empty((batch, 64), dtype=torch.bfloat16, device=dev)
         xt = torch.empty((64, batch), dtype=torch.bfloat16, device=dev)
         tgt = torch.empty((batch, 3), dtype=torch.float32, device=dev)
-        out = torch.empty((batch, 2), dtype=torch.float32, device=dev)
-        dout = torch.empty_like(out)
         lossv = torch.zeros(1, dtype=torch.float64, device=dev)
         lib = L.lib()
         st = L.stream_ptr()
@@ -135,10 +154,8 @@ class WarmStartMLP:
         for k in range(steps):
             L.check(lib.rq_mlp_sample(L.ptr(S), D, L.ptr(Ut), L.ptr(psi), P, seed, k, batch,
                                       L.ptr(x), L.ptr(xt), L.ptr(tgt), st), 'rq_mlp_sample')
-            self.forward(x, out)
             want = log_every and (k % log_every == 0 or k == steps - 1)
-            self.loss(out, tgt, dout, lossv if want else None)
-            self.backward(xt, dout)
+            self.train_step(x, xt, tgt, loss=lossv if want else None)
             frac = k / max(1, steps - 1)
             self.step(lr_min + 0.5 * (lr - lr_min) * (1. + math.cos(math.pi * frac)))
             if want:
@@ -154,7 +171,7 @@ class WarmStartMLP:
         x = torch.empty((D, 64), dtype=torch.bfloat16, device=dev)
         L.check(L.lib().rq_mlp_features(L.ptr(S), D, float(U), L.ptr(x), L.stream_ptr()),
                 'rq_mlp_features')
-        return self.forward(x, out)
+        return self.infer(x, out)
 
     def warm_start(self, states, U, dtype=torch.float64):
         """Start vector sign * exp(log-amplitude) on every state for one U."""

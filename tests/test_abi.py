@@ -73,7 +73,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(L.Operator) == 112 + 56 + 8 + 40 + 8
     assert ctypes.sizeof(L.LobpcgParams) == 64
     assert ctypes.sizeof(L.LobpcgResult) == 48
-    assert ctypes.sizeof(L.Batch) == 208
+    assert ctypes.sizeof(L.Batch) == 240
     assert L.Batch.terms.offset == 80 and L.Batch.nnz.offset == 184
     assert ctypes.sizeof(L.Mlp) == 56
 

@@ -59,9 +59,9 @@ def _reference_forward(m, x):
     import torch.nn.functional as F
     W1, b1, W2, b2, W3, b3 = m.views()
     z1 = x.float() @ m.w1b.float().T + b1
-    h1b = F.gelu(z1).to(torch.bfloat16).float()
+    h1b = F.gelu(z1, approximate='tanh').to(torch.bfloat16).float()
     z2 = h1b @ m.w2b.float().T + b2
-    out = F.gelu(z2) @ W3.T + b3
+    out = F.gelu(z2, approximate='tanh') @ W3.T + b3
     return out, z1, h1b, z2
 
 
@@ -90,6 +90,7 @@ def test_features_match_host_restatement():
 
 @pytest.mark.parametrize('rows', [128, 1000, 4096])
 def test_forward_matches_torch(rows):
+    import torch
     from rqutils_gb300.warmstart import WarmStartMLP
     m = WarmStartMLP(seed=3)
     x = _features(rows, rows)
@@ -98,6 +99,8 @@ def test_forward_matches_torch(rows):
     m.check_errors()
     err = (out - ref).abs().max().item()
     assert err < 2e-3 * max(1., ref.abs().max().item()), err
+    # inference without the stored activations gives the same outputs bit for bit
+    assert torch.equal(m.infer(x), out)
 
 
 def test_backward_matches_torch():
@@ -119,14 +122,16 @@ def test_backward_matches_torch():
     W1, b1, W2, b2, W3, b3 = m.views()
     _, z1, h1b, z2 = _reference_forward(m, x)
 
-    def dgelu(z):
-        return 0.5 * (1 + torch.erf(z / math.sqrt(2))) + z * torch.exp(-0.5 * z * z) / math.sqrt(2 * math.pi)
+    def dgelu(z):  # derivative of the tanh form of GELU
+        k0, k1 = math.sqrt(2 / math.pi), 0.044715
+        t = torch.tanh(k0 * (z + k1 * z ** 3))
+        return 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * k0 * (1 + 3 * k1 * z * z)
 
     z2b = z2.to(torch.bfloat16).float()
     dz2 = (dout @ W3) * dgelu(z2b)
     dz2b = dz2.to(torch.bfloat16).float()
     ref = torch.zeros(NPARAMS, dtype=torch.float32, device='cuda')
-    ref[OFF_W3:OFF_B3] = (dout.T @ F.gelu(z2b)).reshape(-1)
+    ref[OFF_W3:OFF_B3] = (dout.T @ F.gelu(z2b, approximate='tanh')).reshape(-1)
     ref[OFF_B3:] = dout.sum(0)
     ref[OFF_B2:OFF_W3] = dz2.sum(0)
     ref[OFF_W2:OFF_B2] = (dz2b.T @ h1b).reshape(-1)
@@ -137,6 +142,49 @@ def test_backward_matches_torch():
                        (OFF_B2, OFF_W3, 'b2'), (OFF_W3, OFF_B3, 'W3'), (OFF_B3, NPARAMS, 'b3')]:
         e = (m.grads[a:b] - ref[a:b]).norm().item() / max(ref[a:b].norm().item(), 1e-30)
         assert e < 2e-2, (name, e)
+
+
+@pytest.mark.parametrize('rows', [128, 4096, 20480])
+def test_fused_train_step_matches_separate_calls(rows):
+    """rq_mlp_train (loss and head backward in layer 2's epilogue, split-K weight gradients)
+    against rq_mlp_fwd + rq_mlp_loss + rq_mlp_bwd on the same minibatch: the same loss and
+    outputs, and gradients equal up to the BF16 rounding of Z2 that only the separate path does."""
+    import torch
+    from rqutils_gb300.warmstart import (OFF_B1, OFF_B2, OFF_B3, OFF_W1, OFF_W2, OFF_W3,
+                                         NPARAMS, WarmStartMLP)
+    m = WarmStartMLP(seed=14)
+    x = _features(rows, 21) if rows <= 4096 else _features(4096, 21).repeat(rows // 4096, 1)
+    g = torch.Generator().manual_seed(22)
+    tgt = torch.stack([torch.randn(rows, generator=g) - 2.,
+                       torch.where(torch.rand(rows, generator=g) < 0.5, -1., 1.),
+                       torch.rand(rows, generator=g) * 2. + 0.05], 1).cuda()
+    xt = x.T.contiguous()
+    out = m.forward(x)
+    loss_a = torch.zeros(1, dtype=torch.float64, device='cuda')
+    dout = m.loss(out, tgt, loss=loss_a)
+    m.backward(xt, dout)
+    ga = m.grads.clone()
+    out_b = torch.empty_like(out)
+    loss_b = torch.zeros(1, dtype=torch.float64, device='cuda')
+    m.train_step(x, xt, tgt, out=out_b, loss=loss_b)
+    torch.cuda.synchronize()
+    m.check_errors()
+    assert torch.allclose(out_b, out, rtol=0, atol=1e-5)
+    o, t = out.double(), tgt.double()
+    z = -t[:, 1] * o[:, 1]
+    loss_ref = (t[:, 2] * ((o[:, 0] - t[:, 0]) ** 2 + torch.nn.functional.softplus(z))).mean()
+    assert abs(loss_a.item() - loss_ref.item()) <= 1e-5 * abs(loss_ref.item())
+    assert abs(loss_b.item() - loss_a.item()) <= 1e-6 * abs(loss_a.item())
+    gb = m.grads
+    for a, b, name in [(OFF_W1, OFF_B1, 'W1'), (OFF_B1, OFF_W2, 'b1'), (OFF_W2, OFF_B2, 'W2'),
+                       (OFF_B2, OFF_W3, 'b2'), (OFF_W3, OFF_B3, 'W3'), (OFF_B3, NPARAMS, 'b3')]:
+        e = (gb[a:b] - ga[a:b]).norm().item() / max(ga[a:b].norm().item(), 1e-30)
+        assert e < 1e-2, (name, e)
+    # the weight gradients are deterministic: a second call gives the same bits
+    g1 = gb.clone()
+    m.train_step(x, xt, tgt)
+    torch.cuda.synchronize()
+    assert torch.equal(m.grads, g1)
 
 
 def test_adam_step_and_bf16_copies():

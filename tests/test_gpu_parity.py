@@ -279,18 +279,31 @@ def test_presence_bitmap_keeps_results(chem40, mode):
             np.testing.assert_array_equal(u, w)
 
 
-def test_presence_bitmap_batched():
+def test_presence_bitmap_and_line_filter_batched():
+    """Batched products with a forced presence bitmap and with the line filter (256 to 1024-bit
+    lines, each problem with its own prefix shift) equal the product with neither, bit for bit,
+    and so do the cached connectivity lists built through them."""
     import torch
     from rqutils_gb300.batch import BatchedSQD
     from rqutils_gb300.workloads import batched_random_problems
     hams, states, ns = batched_random_problems(17, P=6, d_range=(200, 3000), k_range=(50, 200))
-    a = BatchedSQD(hams, states, presence=False)
-    b = BatchedSQD(hams, states, presence=int(a.c.hbits) + 2)
+    a = BatchedSQD(hams, states, presence=False, line_filter=False)
+    b = BatchedSQD(hams, states, presence=int(a.c.hbits) + 2, line_filter=False)
     assert b.pbits > 0
     rng = np.random.default_rng(1)
     x = torch.as_tensor(rng.normal(size=a.D) + 1j * rng.normal(size=a.D)).cuda()
-    assert torch.equal(a.matvec(x), b.matvec(x))
+    ya = a.matvec(x)
+    assert torch.equal(ya, b.matvec(x))
     b.check_errors()
+    for lb in (8, 9, 10):
+        c = BatchedSQD(hams, states, line_filter=True, line_bits=lb)
+        assert c.lmap is not None and c.pbits == 0
+        assert torch.equal(ya, c.matvec(x)), lb
+        c.check_errors()
+    conn_a = BatchedSQD(hams, states, cache_level=(1, 0), presence=False, line_filter=False)
+    conn_c = BatchedSQD(hams, states, cache_level=(1, 0), line_filter=True)
+    assert conn_a.nnz == conn_c.nnz
+    assert torch.equal(conn_a.col, conn_c.col) and torch.equal(conn_a.grp, conn_c.grp)
 
 
 @pytest.mark.parametrize('cache_level', [(1, 0), (1, 2)])
