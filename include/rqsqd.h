@@ -140,7 +140,9 @@ int rq_subspace_sizes(int64_t D, int32_t key_bits, int32_t *hbits);
 int rq_presence_bits(int64_t D, int32_t key_bits, int32_t *pbits);
 
 /* Line-filter size for D states and 2^lwbits bits per line (lwbits 8..10): 2^lbits lines, each
- * holding 2^(lwbits - 7) states on average; the filter takes 2^(lbits + lwbits - 3) bytes. */
+ * holding 2^(lwbits - 7) states on average (lbits at most 37 - lwbits, so that a word index fits
+ * 32 bits: beyond 2^29 states the lines fill fuller); the filter takes 2^(lbits + lwbits - 3)
+ * bytes. */
 int rq_line_filter_bits(int64_t D, int32_t lwbits, int32_t *lbits);
 
 /* Bytes of scratch that rq_matvec / rq_conn_build / rq_dots need for their reductions/scans. */
@@ -242,7 +244,9 @@ typedef struct rq_lobpcg_params {
     int32_t refresh;        /* FAST: recompute A x, A y every `refresh` iterations (0 = 32)  */
     int32_t use_graph;      /* 0: eager launches; 1: one persistent cooperative kernel per
                                precision phase for RQ_MODE_CONN / RQ_MODE_CSR operators, CUDA
-                               graphs of 8 iterations otherwise; 2: CUDA graphs only        */
+                               graphs of 8 iterations otherwise; 2: CUDA graphs only; 3: the
+                               persistent kernel where 1 would use it, eager launches
+                               otherwise (no graph is ever instantiated)                    */
     int32_t jacobi;         /* 1: precondition the residual with (diag(H) - theta)^-1        */
     int32_t guard;          /* 1: where the reference arithmetic gives 0/0 (a degenerate
                                Cardano eigenvector, |s| = 0) take a finite replacement; only
@@ -277,7 +281,9 @@ int rq_lobpcg_solve(const rq_operator_t *op, const rq_lobpcg_params_t *prm, void
  * of the library, held on every GPU that loads it until the process exits; problems whose
  * rq_lobpcg_workspace_size exceeds 8 MiB are rejected with RQ_E_RANGE (about 60,000 rows in
  * complex128, 40,000 with mixed precision).  The call allocates nothing (no cudaMalloc, no
- * cudaFree, no allocating library routine) and synchronises the stream.  The first call on a
+ * cudaFree, no allocating library routine, no CUDA graph) and synchronises the stream; it runs
+ * with use_graph = 3 whatever prm->use_graph says: cached-connectivity and CSR operators get the
+ * persistent kernel, others eager launches.  The first call on a
  * device looks up the array's device address (once per device); make that first call before any
  * stream capture.  All calls share the array and it keeps the last call's contents (the solver
  * clears what must start at zero): calls that overlap on the GPU (other streams, other threads)

@@ -1758,7 +1758,7 @@ int run_persist_batch(PH &ph, int variant, cudaStream_t s) {
 template <typename PH>
 int run_iterations(PH &ph, int variant, bool graph, int chunk, cudaStream_t s) {
     if constexpr (std::is_same<typename std::decay<decltype(ph.seg)>::type, SegOne>::value) {
-        if (graph && ph.pop && ph.bar) return run_persist(ph, variant, s);
+        if (ph.pop && ph.bar) return run_persist(ph, variant, s);  // set only where allowed
     }
     if constexpr (std::is_same<typename std::decay<decltype(ph.seg)>::type, SegBatch>::value) {
         if (graph && ph.bp) return run_persist_batch(ph, variant, s);
@@ -1865,9 +1865,12 @@ int solve(const rq_operator_t &op, MV mv, bool callback, const rq_lobpcg_params_
                               carve_vecs<VLO>(ws + (mixed ? L.vec_lo : L.vec_hi), L.lo_bytes),
                               jac, op.diag0};
     std::vector<int> nlo;
-    const bool graph = p.use_graph != 0 && !callback;
+    // use_graph 1: persistent kernel where the operator allows it, else graph chunks; 2: graph
+    // chunks only; 3: persistent kernel where allowed, else eager launches (no graph); 0: eager
+    const bool graph = (p.use_graph == 1 || p.use_graph == 2) && !callback;
+    const bool persist = (p.use_graph == 1 || p.use_graph == 3) && !callback;
     // (the Jacobi preconditioner measured slower inside the persistent kernel: graphs then)
-    if (graph && p.use_graph != 2 && !jac && (op.mode == RQ_MODE_CONN || op.mode == RQ_MODE_CSR)) {
+    if (persist && !jac && (op.mode == RQ_MODE_CONN || op.mode == RQ_MODE_CSR)) {
         // one persistent kernel per phase; CSR values must be of the phase's own type
         GridBar *bar = reinterpret_cast<GridBar *>(ws + L.err + 16);
         if (op.mode == RQ_MODE_CONN || op.val_vtype == hi_type) {
@@ -1939,7 +1942,7 @@ int solve_entry(const rq_operator_t *op, rq_matvec_fn fn, void *ctx, const rq_lo
     // after the caller's work
     cudaStream_t s = user;
     cudaStream_t priv = nullptr;
-    const bool graph = prm->use_graph && !fn;
+    const bool graph = (prm->use_graph == 1 || prm->use_graph == 2) && !fn;  // may capture a graph
     if (graph && user == nullptr) {
         RQ_CUDA(cudaStreamCreateWithFlags(&priv, cudaStreamNonBlocking));
         RQ_CUDA(cudaDeviceSynchronize());
@@ -2051,11 +2054,13 @@ RQ_API int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_para
                         std::to_string(kNoallocBytes) + " bytes (use rq_lobpcg_solve)");
     void *ws = nullptr;
     RQ_TRY(noalloc_workspace(&ws));
-    // No CUDA graph of its own: instantiating one may allocate device memory.  The workspace
-    // carries the last call's contents; solve() clears the reduction counter and the error
-    // record it relies on.
+    // No CUDA graph of its own: instantiating one may allocate device memory.  Cached-connectivity
+    // and CSR operators run each precision phase as the persistent cooperative kernel (a launch
+    // that allocates nothing), others launch every pass eagerly.  The workspace carries the last
+    // call's contents; solve() clears the reduction counter, the grid barrier and the error record
+    // it relies on.
     rq_lobpcg_params_t p = *prm;
-    p.use_graph = 0;
+    p.use_graph = 3;
     return solve_entry(op, nullptr, nullptr, &p, ws, x0, x_out, res, stream);
 }
 

@@ -197,13 +197,21 @@ __shared__ uint32_t hk_fb[RQ_FILTER_WORDS];
 __shared__ uint32_t hk_htab[kHashTableWords];
 extern __shared__ __align__(16) unsigned char hk_dyn[];
 
+// Line-filter word of a key (a state or an X mask): the word index line << (lwbits - 5) | word
+// within the line, line = h(k >> lshift) >> (32 - lbits), word = (h(k) mod 2^lwbits) >> 5.  Every
+// step is linear over XOR, so the word of a target s ^ x is word(s) ^ word(x) (lbits + lwbits - 5
+// <= 32 bits, rq_line_filter_bits).
+__device__ __forceinline__ uint32_t line_word(uint32_t h, uint32_t hpre, const rq_subspace_t &S) {
+    return ((hpre >> (32 - S.lbits)) << (S.lwbits - 5)) | ((h & ((1u << S.lwbits) - 1u)) >> 5);
+}
+
 // Group keys of resident indices [c0, c0 + cn) into shared-memory slots [0, cn); the layout holds
-// kt slots (32-bit keys: (x, h(x)) pairs; 64-bit keys: x masks, then hashes; then the line hashes
-// h(x >> lshift)).  Resident index c is group c + (c >= diag_group).  All threads of the block
-// call it.
+// kt slots (32-bit keys: (x, h(x)) pairs; 64-bit keys: x masks, then hashes; then, with the line
+// filter, the line-filter words of the X masks).  Resident index c is group c + (c >= diag_group).
+// All threads of the block call it.
 template <int KB>
 __device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int cn, int kt,
-                                                int lshift) {
+                                                const rq_subspace_t &S) {
     constexpr int NB = KeyWidth<KB>::kNbytes;
     const int skip = T.diag_group;
     uint32_t *hl = reinterpret_cast<uint32_t *>(hk_dyn + group_line_offset<KB>(kt));
@@ -217,7 +225,7 @@ __device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int
             reinterpret_cast<uint64_t *>(hk_dyn)[c] = xv;
             reinterpret_cast<uint32_t *>(hk_dyn + align16((size_t)kt * 8))[c] = h;
         }
-        hl[c] = lin_hash(hk_htab, lshift < 64 ? xv >> lshift : 0ULL, NB);
+        hl[c] = S.lmap ? line_word(h, lin_hash(hk_htab, S.lshift < 64 ? xv >> S.lshift : 0ULL, NB), S) : 0u;
     }
 }
 
@@ -268,9 +276,6 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
     const int pshift = 32 - S.pbits;
     const unsigned char *keys = static_cast<const unsigned char *>(S.hkeys);
     const uint32_t *lmap = S.lmap;
-    const int lsh = 32 - S.lbits;                    // line = (h(s >> lshift) ^ hl_j) >> lsh
-    const int lwsh = S.lwbits - 5;                   // words per line, log2
-    const uint32_t lbmask = (1u << S.lwbits) - 1u;  // bit within the line: h(t) & lbmask
     auto sector = [&](K t) -> bool {
         if (FM == kFiltPoint) {
             int pa, pb;
@@ -298,7 +303,8 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
         const uint64_t s64 = __ldg(S.states + ir);
         const K s = (K)s64;
         const uint32_t hs = lin_hash(hk_htab, s64, NB);
-        const uint32_t hls = LF ? lin_hash(hk_htab, S.lshift < 64 ? s64 >> S.lshift : 0ULL, NB) : 0u;
+        // the row's line-filter word: a target's word is wrow ^ hl[j], its bit (hs ^ h(x)) mod 32
+        const uint32_t wrow = LF ? line_word(hs, lin_hash(hk_htab, S.lshift < 64 ? s64 >> S.lshift : 0ULL, NB), S) : 0u;
         CAcc<R> acc;
         const cx<R> xi = VT<V>::ld(x, ir);
         if (d0) {
@@ -311,7 +317,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
             const int tn = TL ? min(kt, nres - t0) : nres;
             if (tiled) {
                 __syncthreads();  // the previous tile is no longer read
-                load_group_keys<KB>(T, t0, tn, kt, S.lshift);
+                load_group_keys<KB>(T, t0, tn, kt, S);
                 __syncthreads();
             }
             for (int gs0 = 0; gs0 < tn; gs0 += 64) {
@@ -335,7 +341,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
                         }
                         q[u] = sector(t[u]);
                         b[u] = hs ^ hxg;
-                        if (LF) ln[u] = (hls ^ ghl[g + u]) >> lsh;
+                        if (LF) ln[u] = wrow ^ ghl[g + u];
                     }
                     if (pmap) {  // presence bitmap (L2-resident) in front of a table that is not
                         uint32_t pw[U];
@@ -356,8 +362,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
                         uint32_t w[U];
 #pragma unroll
                         for (int u = 0; u < U; ++u)
-                            w[u] = load_word(lmap + ((size_t)ln[u] << lwsh) + ((b[u] & lbmask) >> 5),
-                                             q[u]);
+                            w[u] = load_word(lmap + ln[u], q[u]);
 #pragma unroll
                         for (int u = 0; u < U; ++u)
                             if ((w[u] >> (b[u] & 31u)) & 1u) hb |= 1u << u;
@@ -413,7 +418,7 @@ k_matvec_hash(const rq_operator_t op, const V *__restrict__ x, V *__restrict__ y
     __syncthreads();
     const int nres = T.J - (T.diag_group >= 0 ? 1 : 0);
     if (nres <= max_resident_groups<KB>())  // else in tiles
-        load_group_keys<KB>(T, 0, nres, nres, S.lshift);
+        load_group_keys<KB>(T, 0, nres, nres, S);
     __syncthreads();
     if (FM == kFiltPoint)
         hash_rows<V, KB, FM, LF, BLOCK == 1024>(op, x, y, err, S.fpoint / 65, S.fpoint % 65);

@@ -318,7 +318,9 @@ RQ_API int rq_line_filter_bits(int64_t D, int32_t lwbits, int32_t *lbits) {
     const int64_t lines = (D + per - 1) / per;
     int b = 1;
     while ((int64_t(1) << b) < lines) ++b;
-    if (b > 31) return fail(RQ_E_RANGE, "rq_line_filter_bits: D too large");
+    // at most 2^(37 - lwbits) lines, so that the index of a word (line << (lwbits - 5) | word in
+    // the line) fits 32 bits; only subspaces of more than 2^29 states fill their lines fuller
+    if (b > 37 - lwbits) b = 37 - lwbits;
     *lbits = b;
     return RQ_OK;
 }
@@ -354,8 +356,8 @@ RQ_API int rq_subspace_build(rq_subspace_t *sub, void *scratch, void *stream) {
     int *flag = scratch_err(scratch);
     unsigned long long *gap = reinterpret_cast<unsigned long long *>(scratch);
     if (sub->lookup == RQ_LOOKUP_HASH && sub->lmap &&
-        (sub->lbits < 1 || sub->lbits > 31 || sub->lwbits < 8 || sub->lwbits > 10))
-        return fail(RQ_E_ARG, "rq_subspace_build: line filter needs 1 <= lbits <= 31, 8 <= lwbits <= 10");
+        (sub->lbits < 1 || sub->lwbits < 8 || sub->lwbits > 10 || sub->lbits + sub->lwbits > 37))
+        return fail(RQ_E_ARG, "rq_subspace_build: line filter needs 8 <= lwbits <= 10, 1 <= lbits <= 37 - lwbits");
     if (sub->lookup == RQ_LOOKUP_HASH && sub->pbits != 0 &&
         (!sub->pmap || sub->pbits < 5 || sub->pbits > 32 || sub->pbits < sub->hbits))
         return fail(RQ_E_ARG, "rq_subspace_build: presence bitmap missing or pbits out of range");

@@ -62,11 +62,14 @@ def _solve_noalloc(op, x0, prm):
     return res, xo
 
 
-@pytest.mark.parametrize('name,mixed', [('local12', 0), ('hubbard2x2', 0), ('n16dense', 1)])
-def test_noalloc_matches_workspace_solve(name, mixed):
+@pytest.mark.parametrize('name,mixed,cache_level', [('local12', 0, (1, 0)), ('hubbard2x2', 0, (1, 0)),
+                                                   ('n16dense', 1, (1, 0)), ('hubbard2x2', 1, (0, 0))])
+def test_noalloc_matches_workspace_solve(name, mixed, cache_level):
+    """Cached connectivity runs the persistent kernel in both calls; the matrix-free operator runs
+    eager launches in the allocation-free call and CUDA-graph chunks in the workspace call."""
     import torch
     from rqutils_gb300 import _lib as L
-    prob = _operator(name)
+    prob = _operator(name, cache_level)
     x0 = prob.initial_vector()
     vt = L.F64 if prob.terms.is_real else L.C128
     prm = L.LobpcgParams(maxiter=1000, variant=L.LOBPCG_REFERENCE, vtype=vt, mixed=mixed,
