@@ -29,11 +29,12 @@ def _gemm(A, B, K):
 
 
 @pytest.mark.parametrize('N', [64, 256])
-@pytest.mark.parametrize('M,K,lda', [(128, 64, 64), (300, 192, 192), (257, 128, 256)])
+@pytest.mark.parametrize('M,K,lda', [(128, 64, 64), (300, 192, 192), (257, 128, 256), (500, 512, 520),
+                                     (64, 320, 320)])
 def test_bf16_gemm_exact_on_small_integers(N, M, K, lda):
     """Integer operands in [-3, 3]: every product and partial sum is exact in FP32, so the
     tensor-core result must equal the FP32 product bit for bit (layouts, descriptors, K loop,
-    ragged row tile)."""
+    ragged row tile; B kept in shared memory for K <= 256, streamed with A beyond, a 64-row A)."""
     import torch
     g = torch.Generator().manual_seed(M + N + K)
     Afull = torch.randint(-3, 4, (M, lda), generator=g).to(torch.bfloat16).cuda()
