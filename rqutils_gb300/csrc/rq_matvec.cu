@@ -190,8 +190,10 @@ __host__ __device__ inline size_t group_line_offset(int kt) {
 // Sector filter of the hash kernel: none, the general (popcount a, popcount b) bitset, or the
 // common case of a subspace in one sector (a single bit set: two popcount compares, no table).
 enum { kFiltNone = 0, kFiltSet = 1, kFiltPoint = 2 };
-// line filters of at most 2^26 bytes (64 MB, half of GB300's L2) count as L2-resident
-constexpr int kLineFilterL2Log2Bytes = 26;
+// line filters of at most 2^25 bytes (32 MB, a quarter of GB300's L2) skip the sector test:
+// measured faster without it at 16 MB (Hubbard D = 2^20: 0.089 against 0.107 ms) and slower at
+// 64 MB (chemistry, 2^22 rows: 80.2 against 65.6 ms)
+constexpr int kLineFilterL2Log2Bytes = 25;
 
 // shared memory of the hash kernel: the sector bitset, the hash byte tables (64-bit keys use
 // all eight) and, in dynamic shared memory, the resident group keys
@@ -233,8 +235,8 @@ __device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int
 
 // Probes in flight per thread: four with key buckets (a 16- or 32-byte bucket per probe fills the
 // 40 registers of six resident 256-thread blocks), eight with the line filter (one word per
-// probe) where that fits the registers without spills (ptxas -v): 32-bit keys without the bitset
-// filter.  A divisor of the 64 groups of a super-chunk.
+// probe), four with the line filter and the bitset sector filter (whose registers would spill).
+// A divisor of the 64 groups of a super-chunk.
 #ifndef RQ_LINE_PROBES
 #define RQ_LINE_PROBES 8
 #endif
@@ -242,7 +244,7 @@ constexpr int kKeyProbes = 4;
 
 template <typename V, int KB, int FM>
 constexpr int line_probes() {
-    return (FM == kFiltSet || KB == 64) ? 4 : RQ_LINE_PROBES;
+    return FM == kFiltSet ? 4 : RQ_LINE_PROBES;
 }
 
 // LF: probe the line filter.  TL: the group keys may need streaming in tiles (1024-thread kernels
@@ -756,11 +758,10 @@ int matvec_typed(const rq_operator_t &op, const void *x, void *y, void *scratch,
         case RQ_MODE_FREE:
             if (op.sub.lookup == RQ_LOOKUP_HASH) {
                 // the sector filter is off when both masks are zero; a subspace in one sector
-                // (fpoint >= 0) tests two popcounts instead of the bitset.  Behind a line filter
-                // that stays in L2 the sector test costs more than it saves: a target it would
-                // reject costs one L2 word of the line filter instead (Hubbard D = 2^20: 0.088 ms
-                // without the sector test against 0.107 ms with it); a larger line filter keeps
-                // it, since its words then come from DRAM.
+                // (fpoint >= 0) tests two popcounts instead of the bitset.  Behind a small line
+                // filter the sector test costs more than it saves: a target it would reject
+                // costs one L2-resident word of the line filter instead; a larger line filter
+                // keeps it, since its words then compete for L2 or come from DRAM.
                 const bool line_in_l2 =
                     op.sub.lmap && op.sub.lbits + op.sub.lwbits - 3 <= kLineFilterL2Log2Bytes;
                 const int fm = ((op.sub.fmask_a | op.sub.fmask_b) == 0 || line_in_l2) ? kFiltNone
