@@ -234,17 +234,16 @@ __device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int
 }
 
 // Probes in flight per thread: four with key buckets (a 16- or 32-byte bucket per probe fills the
-// 40 registers of six resident 256-thread blocks), eight with the line filter (one word per
-// probe), four with the line filter and the bitset sector filter (whose registers would spill).
-// A divisor of the 64 groups of a super-chunk.
-#ifndef RQ_LINE_PROBES
-#define RQ_LINE_PROBES 8
-#endif
+// 40 registers of six resident 256-thread blocks).  With the line filter (one 4-byte word per
+// probe): 32 for 32-bit keys without a sector test and in the 1024-thread kernel of 64-bit keys,
+// 8 otherwise, 4 with the bitset sector test: the most that compile without new spills (ptxas -v).
+// 32 against 8 measured 5 % faster on the 64-qubit chemistry subspace (61.7 against 65.4 ms at
+// 2^22 rows) and the same on Hubbard.  A divisor of the 64 groups of a super-chunk.
 constexpr int kKeyProbes = 4;
 
-template <typename V, int KB, int FM>
-constexpr int line_probes() {
-    return FM == kFiltSet ? 4 : RQ_LINE_PROBES;
+template <typename V, int KB, int FM, bool TL>
+__host__ __device__ constexpr int line_probes() {
+    return FM == kFiltSet ? 4 : ((KB == 32 && FM == kFiltNone) || (KB == 64 && TL)) ? 32 : 8;
 }
 
 // LF: probe the line filter.  TL: the group keys may need streaming in tiles (1024-thread kernels
@@ -257,7 +256,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
     using K = typename KeyWidth<KB>::K;
     constexpr int NB = KeyWidth<KB>::kNbytes;
     constexpr int kBucketBytes = KeyWidth<KB>::kBucketBytes;
-    constexpr int U = LF ? line_probes<V, KB, FM>() : kKeyProbes;
+    constexpr int U = LF ? line_probes<V, KB, FM, TL>() : kKeyProbes;
     const rq_subspace_t &S = op.sub;
     const rq_terms_t &T = op.terms;
     const int64_t D = S.D;
