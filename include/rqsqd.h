@@ -85,13 +85,14 @@ typedef struct rq_subspace {
     uint32_t *pmap;          /* [2^pbits / 32]: bit (hash(s) >> (32 - pbits)) set for every
                                 state, written by rq_subspace_build; a lookup whose bit is
                                 clear skips the table (NULL = none)                        */
-    uint32_t *lmap;          /* line filter, [2^lbits lines of 2^lwbits bits] or NULL: bit
-                                (hash(s) mod 2^lwbits) of line (hash(s >> lshift) >> (32 -
-                                lbits)) set for every state, written by rq_subspace_build.
+    uint32_t *lmap;          /* line filter, [2^lbits lines of 2^lwbits bits] or NULL: for
+                                every state, with h = hash(s), bits h mod 32 and h >> 27 of word
+                                (h mod 2^lwbits) >> 5 of line hash(s >> lshift) >> (32 -
+                                lbits), written by rq_subspace_build.
                                 States that agree above bit lshift share a line, and so do
                                 their targets under one X mask: the rows of a warp (consecutive
                                 sorted states) probe a few lines instead of one line per lane.
-                                A clear bit is a miss; a set bit is resolved in the table    */
+                                A clear bit is a miss; two set bits are resolved in the table */
     int32_t   lbits;         /* log2(lines) of lmap, from rq_line_filter_bits               */
     int32_t   lwbits;        /* log2(bits per line): 8 (32-byte lines) .. 10 (128-byte)     */
     int32_t   lshift;        /* written by rq_subspace_build: the prefix shift, chosen so that

@@ -138,7 +138,8 @@ k_batch_line_prep(const uint64_t *__restrict__ keys, const int64_t *__restrict__
     for (int g = gofs[p] + threadIdx.x; g < gofs[p + 1]; g += blockDim.x) xline[g] = lin_hash(T, xmask[g] >> b, 8);
 }
 
-// bit (hash(key) mod 2^lwbits) of line hash(key >> lshift[p]) >> (32 - lbits) for every key
+// for every key (h = hash(key)): bits h mod 32 and h >> 27 of word (h mod 2^lwbits) >> 5 of line
+// hash(key >> lshift[p]) >> (32 - lbits)
 __global__ void __launch_bounds__(kThreads)
 k_batch_line_build(const uint64_t *__restrict__ keys, int64_t D, const int32_t *__restrict__ lshift,
                    uint32_t *__restrict__ lmap, int lbits, int lwbits) {
@@ -149,8 +150,8 @@ k_batch_line_build(const uint64_t *__restrict__ keys, int64_t D, const int32_t *
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t k = keys[i];
         const uint32_t line = lin_hash(T, k >> lshift[problem_of(k)], 8) >> (32 - lbits);
-        const uint32_t bit = lin_hash(T, k, 8) & bmask;
-        atomicOr(lmap + ((size_t)line << (lwbits - 5)) + (bit >> 5), 1u << (bit & 31));
+        const uint32_t h = lin_hash(T, k, 8);
+        atomicOr(lmap + ((size_t)line << (lwbits - 5)) + ((h & bmask) >> 5), (1u << (h & 31)) | (1u << (h >> 27)));
     }
 }
 
@@ -241,7 +242,7 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
                     lw[u] = q[u] ? __ldg(B.lmap + ((size_t)ln << lwsh) + ((b[u] & lbmask) >> 5)) : 0u;
                 }
 #pragma unroll
-                for (int u = 0; u < U; ++u) q[u] = q[u] && ((lw[u] >> (b[u] & 31)) & 1u);
+                for (int u = 0; u < U; ++u) q[u] = q[u] && ((lw[u] >> (b[u] & 31)) & (lw[u] >> (b[u] >> 27)) & 1u);
             } else if (B.pbits > 0) {
                 uint32_t pw[U];
 #pragma unroll

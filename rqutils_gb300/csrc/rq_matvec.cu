@@ -235,15 +235,16 @@ __device__ __forceinline__ void load_group_keys(const rq_terms_t &T, int c0, int
 
 // Probes in flight per thread: four with key buckets (a 16- or 32-byte bucket per probe fills the
 // 40 registers of six resident 256-thread blocks).  With the line filter (one 4-byte word per
-// probe): 32 for 32-bit keys without a sector test and in the 1024-thread kernel of 64-bit keys,
+// probe): 32 for 32-bit keys without a sector test, 16 in the 1024-thread kernel of 64-bit keys,
 // 8 otherwise, 4 with the bitset sector test: the most that compile without new spills (ptxas -v).
-// 32 against 8 measured 5 % faster on the 64-qubit chemistry subspace (61.7 against 65.4 ms at
-// 2^22 rows) and the same on Hubbard.  A divisor of the 64 groups of a super-chunk.
+// More probes in flight measured 5 % faster on the 64-qubit chemistry subspace (61.7 against
+// 65.4 ms at 2^22 rows, one-bit filter) and the same on Hubbard.  A divisor of the 64 groups of a
+// super-chunk.
 constexpr int kKeyProbes = 4;
 
 template <typename V, int KB, int FM, bool TL>
 __host__ __device__ constexpr int line_probes() {
-    return FM == kFiltSet ? 4 : ((KB == 32 && FM == kFiltNone) || (KB == 64 && TL)) ? 32 : 8;
+    return FM == kFiltSet ? 4 : (KB == 32 && FM == kFiltNone) ? 32 : (KB == 64 && TL) ? 16 : 8;
 }
 
 // LF: probe the line filter.  TL: the group keys may need streaming in tiles (1024-thread kernels
@@ -368,7 +369,7 @@ __device__ __forceinline__ void hash_rows(const rq_operator_t &op, const V *__re
                             w[u] = load_word(lmap + ln[u], q[u]);
 #pragma unroll
                         for (int u = 0; u < U; ++u)
-                            if ((w[u] >> (b[u] & 31u)) & 1u) hb |= 1u << u;
+                            if ((w[u] >> (b[u] & 31u)) & (w[u] >> (b[u] >> 27)) & 1u) hb |= 1u << u;
                     } else {
                         typename KeyWidth<KB>::Bucket w[U];
 #pragma unroll

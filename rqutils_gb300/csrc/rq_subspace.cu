@@ -107,9 +107,11 @@ __global__ void k_prefix_hist(const uint64_t *__restrict__ s, int64_t D,
     if (threadIdx.x < 64 && h[threadIdx.x]) atomicAdd(hist + threadIdx.x, (unsigned long long)h[threadIdx.x]);
 }
 
-// Line filter: for every state, bit (hash(s) mod 2^lwbits) of line hash(s >> lshift) >> (32 -
-// lbits).  Both hashes are the GF(2)-linear lookup hash, so a target's line and bit follow from
-// the row's and the X mask's by XOR.
+// Line filter: for every state s with h = hash(s), word (h mod 2^lwbits) >> 5 of line
+// hash(s >> lshift) >> (32 - lbits), bits h mod 32 and h >> 27 of that word (two bits of one word:
+// a probe loads one word and a miss passes both tests with probability ~(1/64)^2).  Both hashes are
+// the GF(2)-linear lookup hash, so a target's line, word and bits follow from the row's and the X
+// mask's by XOR.
 template <int KB>
 __global__ void __launch_bounds__(kThreads)
 k_line_build(const uint64_t *__restrict__ s, int64_t D, uint32_t *__restrict__ lmap, int lbits,
@@ -122,8 +124,8 @@ k_line_build(const uint64_t *__restrict__ s, int64_t D, uint32_t *__restrict__ l
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t k = s[i];
         const uint32_t line = lin_hash(T, lshift < 64 ? k >> lshift : 0ULL, KeyWidth<KB>::kNbytes) >> (32 - lbits);
-        const uint32_t bit = lin_hash(T, k, KeyWidth<KB>::kNbytes) & bmask;
-        atomicOr(lmap + ((size_t)line << (lwbits - 5)) + (bit >> 5), 1u << (bit & 31));
+        const uint32_t h = lin_hash(T, k, KeyWidth<KB>::kNbytes);
+        atomicOr(lmap + ((size_t)line << (lwbits - 5)) + ((h & bmask) >> 5), (1u << (h & 31)) | (1u << (h >> 27)));
     }
 }
 
