@@ -489,6 +489,7 @@ def run_batched(args, rank, ws):
     value = ws * wl.P * args.steps / t_step
     y_conn = b_conn.matvec(x)
     rel = float(torch.linalg.vector_norm(y - y_conn) / torch.linalg.vector_norm(y_conn))
+    y_timed = y.cpu().numpy() if rank == 0 else None  # checked against the oracle below
     for _ in range(args.warmup):
         b_conn.matvec(x, out=y)
     t_conn = statistics.mean(time_steps(lambda: b_conn.matvec(x, out=y), max(3, args.steps),
@@ -559,7 +560,9 @@ def run_batched(args, rank, ws):
         'clocks': clk.summary(),
     }
     if rank == 0:
-        line['cpu_baseline'] = cpu_baseline_batched(wl, budget_s=12.0)
+        cb = cpu_baseline_batched(wl, budget_s=12.0, y_gpu=y_timed)
+        line['cpu_baseline'] = cb
+        line['matvec_rel_err_vs_oracle'] = cb.get('vs_gpu')
         print(json.dumps(line), flush=True)
 
 
@@ -863,27 +866,37 @@ def cpu_baseline(wl, budget_s=12.0, steps=None, y_gpu=None):
     return out
 
 
-def cpu_baseline_batched(wl, budget_s=12.0):
+def cpu_baseline_batched(wl, budget_s=12.0, y_gpu=None):
     """The oracle's apply_h restatement problem by problem (complex128, groups over all cores),
-    on as many problems as fit the budget, scaled to the batch by rows x groups."""
+    on as many problems as fit the budget, scaled to the batch by rows x groups.  With ``y_gpu``
+    (the timed batched GPU product, on the host) its error against the oracle's products of the
+    problems computed is reported as ``vs_gpu``."""
     from oracle.sqd import matvec_nocache
     cores = os.cpu_count() or 1
     work = np.array([len(S) * len(h.xmask) for h, S in zip(wl.hams, wl.S)], dtype=np.float64)
     done, spent, p = 0., 0., 0
+    ys, yg = [], []
     while p < wl.P and spent < budget_s:
         terms = _oracle_setup(wl.hams[p])
         rows = slice(int(sum(len(s) for s in wl.S[:p])), int(sum(len(s) for s in wl.S[:p + 1])))
         xp = wl.x[rows].astype(np.complex128)
         t0 = time.perf_counter()
-        matvec_nocache(xp, terms, wl.S[p], threads=cores)
+        yp = matvec_nocache(xp, terms, wl.S[p], threads=cores)
         spent += time.perf_counter() - t0
+        if y_gpu is not None:
+            ys.append(yp)
+            yg.append(np.asarray(y_gpu)[rows])
         done += work[p]
         p += 1
     dt = spent * work.sum() / done  # seconds for one matvec of every problem
-    return {'value': wl.P / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': f'one matvec of each of the first {p} of {wl.P} problems ({spent:.1f} s), '
-                      'scaled to the batch by rows x groups; complex128, NumPy restatement of '
-                      'apply_h with per-group sort-merge'}
+    out = {'value': wl.P / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+           'sample': f'one matvec of each of the first {p} of {wl.P} problems ({spent:.1f} s), '
+                     'scaled to the batch by rows x groups; complex128, NumPy restatement of '
+                     'apply_h with per-group sort-merge'}
+    if ys:
+        out['vs_gpu'] = dict(_err_vs_oracle(np.concatenate(yg), np.concatenate(ys)),
+                             what=f'the rows of the first {p} problems')
+    return out
 
 
 def run_reference(args, rank, ws):
