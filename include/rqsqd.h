@@ -72,8 +72,9 @@ extern "C" {
 typedef struct rq_subspace {
     const uint64_t *states;  /* [D] strictly increasing                                   */
     int64_t   D;             /* subspace dimension, 1 <= D < 2^31                          */
-    void     *hkeys;         /* 2^hbits buckets of 4 keys: (key_bits / 2) << hbits bytes    */
-    int32_t  *hvals;         /* [4 << hbits] row index of each key slot                    */
+    void     *hkeys;         /* 2^hbits buckets of 4 keys: (key_bits / 2) << hbits bytes,
+                                16-byte aligned                                            */
+    int32_t  *hvals;         /* [4 << hbits] row index of each key slot, 16-byte aligned   */
     int32_t   hbits;         /* log2(number of buckets), from rq_subspace_sizes            */
     int32_t   lookup;        /* RQ_LOOKUP_*                                                */
     int32_t   key_bits;      /* 32: states and every X mask < 2^32 (16-byte buckets); 64   */

@@ -259,9 +259,12 @@ __device__ __forceinline__ int lookup_hash_at(const rq_subspace_t &S, uint64_t t
                                               int *err) {
     using K = typename KeyWidth<KB>::K;
     if (t == S.empty_key || (KB == 32 && (t >> 32) != 0)) return -1;
+    // the bucket's four row indices load beside its keys (independent addresses; hvals is 16-byte
+    // aligned), so a hit costs one round trip to the table instead of two
+    const int4 v = __ldg(reinterpret_cast<const int4 *>(S.hvals) + b);
     const auto bk = KeyWidth<KB>::load(bucket_ptr<KB>(S, b), true, S.empty_key);
     const int s = slot_of(bk, (K)t);
-    if (s >= 0) return S.hvals[(size_t)b * kBucketSlots + s];
+    if (s >= 0) return s == 0 ? v.x : s == 1 ? v.y : s == 2 ? v.z : v.w;
     if (bk.k[3] == (K)S.empty_key) return -1;
     return probe_rest<KB>(S, t, b, err);
 }

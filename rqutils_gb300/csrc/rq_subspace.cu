@@ -239,6 +239,9 @@ int grid_for(int64_t n, int per_sm = 8) {
 int build_key_table(const uint64_t *keys, int64_t D, int key_bits, bool hash, void *hkeys,
                     int32_t *hvals, int hbits, uint64_t *empty_out, int *flag,
                     unsigned long long *gap, cudaStream_t st, uint32_t *pmap, int pbits) {
+    // buckets (keys) and their four row indices are read as vectors
+    if (hash && (reinterpret_cast<uintptr_t>(hkeys) % 16 != 0 || reinterpret_cast<uintptr_t>(hvals) % 16 != 0))
+        return fail(RQ_E_ARG, "hash table arrays (hkeys, hvals) must be 16-byte aligned");
     RQ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     RQ_CUDA(cudaMemsetAsync(gap, 0xff, sizeof(unsigned long long), st));
     k_check_sorted<<<grid_for(D), kThreads, 0, st>>>(keys, D, flag);
