@@ -218,50 +218,64 @@ __device__ __forceinline__ void batch_row_hits(const rq_batch_t &B, const uint32
             }
         }
         uint64_t hot = 0ULL;
-        while (__any_sync(0xffffffffu, pass != 0ULL)) {
-            int rr[U];
-            uint64_t t[U];
-            uint32_t b[U];
-            bool q[U];
-            typename KeyWidth<64>::Bucket w[U];
+        if (xl) {
+            // line filter: a group whose target sets both bits is resolved below (the lookup
+            // reads its bucket), so only filter words are in flight, eight per thread
+            constexpr int UL = 8;
+            while (__any_sync(0xffffffffu, pass != 0ULL)) {
+                int rr[UL];
+                uint32_t b[UL], lw[UL];
+                bool q[UL];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                q[u] = pass != 0ULL;
-                rr[u] = q[u] ? __ffsll((long long)pass) - 1 : 0;
-                pass &= pass - 1ULL;
-                const uint64_t xv = q[u] ? __ldg(xm + r0 + rr[u]) : 0ULL;
-                const uint32_t hx = q[u] ? __ldg(xh + r0 + rr[u]) : 0u;
-                t[u] = key ^ xv;
-                b[u] = hs ^ hx;
-            }
-            if (xl) {
-                uint32_t lw[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
+                for (int u = 0; u < UL; ++u) {
+                    q[u] = pass != 0ULL;
+                    rr[u] = q[u] ? __ffsll((long long)pass) - 1 : 0;
+                    pass &= pass - 1ULL;
+                    b[u] = hs ^ (q[u] ? __ldg(xh + r0 + rr[u]) : 0u);
                     const uint32_t ln = q[u] ? (hls ^ __ldg(xl + r0 + rr[u])) >> lsh : 0u;
                     lw[u] = q[u] ? __ldg(B.lmap + ((size_t)ln << lwsh) + ((b[u] & lbmask) >> 5)) : 0u;
                 }
 #pragma unroll
-                for (int u = 0; u < U; ++u) q[u] = q[u] && ((lw[u] >> (b[u] & 31)) & (lw[u] >> (b[u] >> 27)) & 1u);
-            } else if (B.pbits > 0) {
-                uint32_t pw[U];
+                for (int u = 0; u < UL; ++u)
+                    if (q[u] && ((lw[u] >> (b[u] & 31)) & (lw[u] >> (b[u] >> 27)) & 1u)) hot |= 1ULL << rr[u];
+            }
+        } else {
+            while (__any_sync(0xffffffffu, pass != 0ULL)) {
+                int rr[U];
+                uint64_t t[U];
+                uint32_t b[U];
+                bool q[U];
+                typename KeyWidth<64>::Bucket w[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    const uint32_t idx = b[u] >> (32 - B.pbits);
-                    pw[u] = q[u] ? __ldg(B.pmap + (idx >> 5)) : 0u;
+                    q[u] = pass != 0ULL;
+                    rr[u] = q[u] ? __ffsll((long long)pass) - 1 : 0;
+                    pass &= pass - 1ULL;
+                    const uint64_t xv = q[u] ? __ldg(xm + r0 + rr[u]) : 0ULL;
+                    const uint32_t hx = q[u] ? __ldg(xh + r0 + rr[u]) : 0u;
+                    t[u] = key ^ xv;
+                    b[u] = hs ^ hx;
+                }
+                if (B.pbits > 0) {
+                    uint32_t pw[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const uint32_t idx = b[u] >> (32 - B.pbits);
+                        pw[u] = q[u] ? __ldg(B.pmap + (idx >> 5)) : 0u;
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+                        q[u] = q[u] && ((pw[u] >> ((b[u] >> (32 - B.pbits)) & 31)) & 1u);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    q[u] = q[u] && ((pw[u] >> ((b[u] >> (32 - B.pbits)) & 31)) & 1u);
-            }
+                    w[u] = KeyWidth<64>::load(keys + (size_t)(b[u] >> shift) * 32, q[u], B.empty_key);
 #pragma unroll
-            for (int u = 0; u < U; ++u)
-                w[u] = KeyWidth<64>::load(keys + (size_t)(b[u] >> shift) * 32, q[u], B.empty_key);
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                bool any, open;
-                test_bucket(w[u], t[u], B.empty_key, any, open);
-                if (q[u] && (any || !open)) hot |= 1ULL << rr[u];
+                for (int u = 0; u < U; ++u) {
+                    bool any, open;
+                    test_bucket(w[u], t[u], B.empty_key, any, open);
+                    if (q[u] && (any || !open)) hot |= 1ULL << rr[u];
+                }
             }
         }
         while (hot) {
