@@ -64,6 +64,15 @@ def test_host_only_entry_points(libpath):
     assert n.value >= 8 * 1000 * 24
     assert lib.rq_subspace_sizes(0, 64, ctypes.byref(hb)) == L.E_ARG
     assert b'D must be' in lib.rq_last_error()
+    # line filter: two states per 256-bit line, 2^(lbits + lwbits - 3) bytes; at most 2^(37 -
+    # lwbits) lines, so that a word index fits 32 bits
+    lb = ctypes.c_int32()
+    assert lib.rq_line_filter_bits(1 << 20, 8, ctypes.byref(lb)) == 0 and lb.value == 19
+    assert lib.rq_line_filter_bits(1 << 20, 10, ctypes.byref(lb)) == 0 and lb.value == 17
+    assert lib.rq_line_filter_bits(3, 8, ctypes.byref(lb)) == 0 and lb.value == 1
+    assert lib.rq_line_filter_bits((1 << 31) - 1, 8, ctypes.byref(lb)) == 0 and lb.value == 29
+    assert lib.rq_line_filter_bits((1 << 31) - 1, 10, ctypes.byref(lb)) == 0 and lb.value == 27
+    assert lib.rq_line_filter_bits(1 << 20, 11, ctypes.byref(lb)) == L.E_ARG
 
 
 def test_struct_layouts():
