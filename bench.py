@@ -416,8 +416,8 @@ def run_ours(args, rank, ws):
     if rank == 0:
         cb = cpu_baseline(wl, budget_s=12.0, y_gpu=y_timed)
         line['cpu_baseline'] = cb
-        # error of the timed product against the oracle's complex128 product (spec bound
-        # 1e-6 relative), computed outside the timed region by the CPU-baseline leg
+        # error of the timed product against the oracle's complex128 product (32-bit products
+        # are held to 1e-6 relative), computed outside the timed region by the CPU-baseline leg
         line['matvec_rel_err_vs_oracle'] = cb.get('vs_gpu')
         print(json.dumps(line), flush=True)
 
