@@ -14,7 +14,8 @@ count and the vector type -- in a ``TuneCache`` (in memory, and in a JSON file w
 a path), so a later problem of the class takes the recorded form without measuring.
 
 ``SQDProblem`` / ``sqd`` and ``BatchedSQD`` accept ``cache_level='auto'``, which uses this module
-(for batches the candidates are the matrix-free and cached-connectivity forms).
+(for batches the candidates are the matrix-free form with the line filter or the presence
+bitmap, and the cached-connectivity form).
 """
 import json
 import math
@@ -175,9 +176,11 @@ def tune(hamiltonian, states, dtype=None, expected_products=400, warmup=2, reps=
 
 def tune_batch(hamiltonians, states_list, dtype=None, expected_products=400, warmup=2, reps=5,
                cache=None, device=None):
-    """Matrix-free or cached connectivity for a batch (BatchedSQD): the same measurement over
-    the batch's two forms (``hamiltonians`` PauliSumXZ, ``states_list`` sorted uint64 arrays).
-    Returns ('free' | 'conn', {form: seconds})."""
+    """Matrix-free (with the line filter or the presence bitmap in front of the table) or cached
+    connectivity for a batch (BatchedSQD): the same measurement over the batch's forms
+    (``hamiltonians`` PauliSumXZ, ``states_list`` sorted uint64 arrays).  Returns
+    ('free' | 'conn', {form: seconds}); the line-filter choice is in the form's line bits
+    (8 = line filter, 0 = presence bitmap)."""
     import torch
     from .batch import BatchedSQD
     cache = cache if cache is not None else _DEFAULT
@@ -189,14 +192,15 @@ def tune_batch(hamiltonians, states_list, dtype=None, expected_products=400, war
     cls = problem_class('batch', n, D, J, dt)
     hit = cache.get(cls)
     if hit is not None:
-        return hit[0], {}
+        return hit, {}
     rng = np.random.default_rng(0)
     times = {}
-    for mode, cl in (('free', (0, 0)), ('conn', (1, 0))):
+    for mode, cl, lb in (('free', (0, 0), 8), ('free', (0, 0), 0), ('conn', (1, 0), 8)):
         try:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            b = BatchedSQD(hamiltonians, states_list, cache_level=cl, device=device)
+            b = BatchedSQD(hamiltonians, states_list, cache_level=cl, device=device,
+                           line_filter=lb > 0, line_bits=lb or 8)
             torch.cuda.synchronize()
             build = time.perf_counter() - t0
         except (RuntimeError, MemoryError):  # a form that does not fit: not a candidate
@@ -204,11 +208,11 @@ def tune_batch(hamiltonians, states_list, dtype=None, expected_products=400, war
             continue
         xr = rng.normal(size=b.D) + (0 if real else 1j) * rng.normal(size=b.D)
         probe = torch.as_tensor(xr).to(b.device, dt)
-        times[(mode, 'hash', 0)] = build + expected_products * _time_products(
+        times[(mode, 'hash', lb)] = build + expected_products * _time_products(
             b.matvec, probe, warmup, reps)
         del b
     if not times:
         raise RuntimeError('autotune: no batched form could be built')
     best = min(times, key=times.get)
     cache.put(cls, best, times)
-    return best[0], times
+    return best, times

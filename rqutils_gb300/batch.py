@@ -98,8 +98,9 @@ class BatchedSQD:
         if cache_level == 'auto':
             from .autotune import tune_batch
             sl = [subspace_states(s, h.num_qubits) for h, s in zip(hams, states_list)]
-            mode, _ = tune_batch(hams, sl, cache=tune_cache, device=self.device)
+            (mode, _, lb), _ = tune_batch(hams, sl, cache=tune_cache, device=self.device)
             cache_level = (0, 0) if mode == 'free' else (1, 0)
+            line_filter = lb > 0
         for h in hams:
             if h.num_qubits > STATE_BITS:
                 raise ValueError(f'batched problems have at most {STATE_BITS} qubits')

@@ -65,6 +65,8 @@ def test_tuned_batch_solves_like_the_fixed_forms():
     cache = TuneCache()
     b = BatchedSQD(hams, states, cache_level='auto', tune_cache=cache)
     assert b.mode in ('free', 'conn') and len(cache.records) == 1
+    # three candidates: matrix-free with the line filter or the presence bitmap, connectivity
+    assert len(next(iter(cache.records.values()))['times']) == 3
     ref = BatchedSQD(hams, states, cache_level=(1, 0))
     rng = np.random.default_rng(93)
     xr = rng.normal(size=b.D) + 1j * rng.normal(size=b.D)
