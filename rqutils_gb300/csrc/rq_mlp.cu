@@ -891,18 +891,31 @@ __global__ void __launch_bounds__(kHid) k_head_bwd(const bf16 *__restrict__ z2, 
     }
 }
 
-// dst[c] = sum_t part[t * ncols + c]: a block of kColsumWarps warps per 32 VW columns (lane =
-// VW consecutive columns, so every row of partials is read in 32 VW-wide coalesced pieces); warp w
-// adds the rows t in its contiguous range with two interleaved accumulators, then warp 0 adds the
-// warp sums in warp order.  The order of every addition is fixed, so the sums are the same on every
-// run.  VW = 4 needs ncols a multiple of 4 and 16-byte aligned rows.
+// dst[c] = sum_t part[t * ncols + c] for up to four sets of partial sums in one launch: a block
+// of kColsumWarps warps per 32 VW columns of one set (lane = VW consecutive columns, so every row
+// of partials is read in 32 VW-wide coalesced pieces); warp w adds the rows t in its contiguous
+// range with two interleaved accumulators, then the warp sums are added in warp order.  The
+// order of every addition is fixed, so the sums are the same on every run.  VW = 4 needs ncols a
+// multiple of 4 and 16-byte aligned rows.
 constexpr int kColsumWarps = 8;
+struct ColsumSet {
+    const float *part;
+    int64_t nt, ncols;
+    float *dst;
+    int vw;      // 4 or 1
+    int blocks;  // blocks of the launch that serve this set
+};
+struct ColsumSets {
+    ColsumSet s[4];
+    int n;
+};
+
 template <int VW>
-__global__ void __launch_bounds__(kColsumWarps * 32)
-k_colsum(const float *__restrict__ part, int64_t nt, int64_t ncols, float *__restrict__ dst) {
-    __shared__ float ws[kColsumWarps][32 * VW + 1];
+__device__ __forceinline__ void colsum_block(const ColsumSet &g, int64_t blk, float (*ws)[32 * 4 + 1]) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t c = ((int64_t)blockIdx.x * 32 + lane) * VW;
+    const int64_t nt = g.nt, ncols = g.ncols;
+    const float *part = g.part;
+    const int64_t c = (blk * 32 + lane) * VW;
     const int64_t t0 = w * nt / kColsumWarps, t1 = (w + 1) * nt / kColsumWarps;
     float a[2][VW] = {};
     if (c < ncols) {
@@ -937,20 +950,39 @@ k_colsum(const float *__restrict__ part, int64_t nt, int64_t ncols, float *__res
     for (int j = 0; j < VW; ++j) ws[w][lane * VW + j] = a[0][j] + a[1][j];
     __syncthreads();
     for (int i = threadIdx.x; i < 32 * VW; i += blockDim.x) {
-        const int64_t ci = (int64_t)blockIdx.x * 32 * VW + i;
+        const int64_t ci = blk * 32 * VW + i;
         if (ci < ncols) {
             float s = 0.f;
             for (int k = 0; k < kColsumWarps; ++k) s += ws[k][i];
-            dst[ci] = s;
+            g.dst[ci] = s;
         }
     }
 }
 
-int launch_colsum(const float *part, int64_t nt, int64_t ncols, float *dst, cudaStream_t st) {
-    if (ncols % 4 == 0 && reinterpret_cast<uintptr_t>(part) % 16 == 0)
-        k_colsum<4><<<(unsigned)((ncols + 127) / 128), kColsumWarps * 32, 0, st>>>(part, nt, ncols, dst);
+__global__ void __launch_bounds__(kColsumWarps * 32) k_colsum(const ColsumSets S) {
+    __shared__ float ws[kColsumWarps][32 * 4 + 1];
+    int64_t b = blockIdx.x;
+    int k = 0;
+    while (k < S.n - 1 && b >= S.s[k].blocks) b -= S.s[k++].blocks;
+    if (S.s[k].vw == 4)
+        colsum_block<4>(S.s[k], b, ws);
     else
-        k_colsum<1><<<(unsigned)((ncols + 31) / 32), kColsumWarps * 32, 0, st>>>(part, nt, ncols, dst);
+        colsum_block<1>(S.s[k], b, ws);
+}
+
+// the column sums of n (<= 4) sets of partials, one launch
+int launch_colsums(const ColsumSet *sets, int n, cudaStream_t st) {
+    ColsumSets S{};
+    S.n = n;
+    int64_t total = 0;
+    for (int k = 0; k < n; ++k) {
+        S.s[k] = sets[k];
+        S.s[k].vw = (sets[k].ncols % 4 == 0 && reinterpret_cast<uintptr_t>(sets[k].part) % 16 == 0) ? 4 : 1;
+        S.s[k].blocks = (int)((sets[k].ncols + 32 * S.s[k].vw - 1) / (32 * S.s[k].vw));
+        total += S.s[k].blocks;
+    }
+    if (n < 1 || n > 4 || total < 1 || total > 0x7FFFFFFF) return fail(RQ_E_RANGE, "column sums: bad sets");
+    k_colsum<<<(unsigned)total, kColsumWarps * 32, 0, st>>>(S);
     RQ_CUDA(cudaGetLastError());
     return RQ_OK;
 }
@@ -1134,13 +1166,12 @@ int backward_tail(const rq_mlp_t *m, int64_t rows, const uint16_t *xt, const Mlp
     b.err = err;
     RQ_TRY((launch_gemm<kHid, EPI_F32>(reinterpret_cast<const bf16 *>(xt), L.Mp,
                                        reinterpret_cast<const bf16 *>(w + L.dz1t), L.Mp, L.Mp, b, st)));
-    RQ_TRY(launch_colsum(reinterpret_cast<const float *>(w + L.split1), L.nsplit1, kHid * kIn,
-                         m->grads + kOffW1, st));
-    RQ_TRY(launch_colsum(reinterpret_cast<const float *>(w + L.colpart1), grid1, kHid, m->grads + kOffB1, st));
-    RQ_TRY(launch_colsum(reinterpret_cast<const float *>(w + L.split2), L.nsplit, kHid * kHid,
-                         m->grads + kOffW2, st));
-    RQ_TRY(launch_colsum(part2, part2_rows, kHeadPart, m->grads + kOffB2, st));
-    return RQ_OK;
+    const ColsumSet sets[4] = {
+        {reinterpret_cast<const float *>(w + L.split1), L.nsplit1, kHid * kIn, m->grads + kOffW1, 0, 0},
+        {reinterpret_cast<const float *>(w + L.colpart1), grid1, kHid, m->grads + kOffB1, 0, 0},
+        {reinterpret_cast<const float *>(w + L.split2), L.nsplit, kHid * kHid, m->grads + kOffW2, 0, 0},
+        {part2, part2_rows, kHeadPart, m->grads + kOffB2, 0, 0}};
+    return launch_colsums(sets, 4, st);
 }
 
 }  // namespace
