@@ -367,6 +367,9 @@ def run_ours(args, rank, ws):
         xr = rng.normal(size=D) if real else rng.normal(size=D) + 1j * rng.normal(size=D)
         variants = [('mixed_fast', dict(mixed=True, variant='fast')),
                     ('fp64_fast', dict(mixed=False, variant='fast')),
+                    # opt-in: the step restarts from x every 100 iterations of a phase
+                    ('mixed_fast_restart100', dict(mixed=True, variant='fast', restart=100)),
+                    ('fp64_fast_restart100', dict(mixed=False, variant='fast', restart=100)),
                     ('fp64_reference', dict(mixed=False, variant='reference'))]
         if wl.name == 'random20':
             # Jacobi helps here; on the Hubbard subspace the diagonal (U x double occupancy) is

@@ -253,6 +253,10 @@ typedef struct rq_lobpcg_params {
     int32_t guard;          /* 1: where the reference arithmetic gives 0/0 (a degenerate
                                Cardano eigenvector, |s| = 0) take a finite replacement; only
                                results that would otherwise be NaN change                    */
+    int32_t restart;        /* FAST, one problem: drop the search direction and restart the
+                               step from x every `restart` iterations of a phase (0 = never;
+                               the reference never restarts)                                  */
+    int32_t pad_;
 } rq_lobpcg_params_t;
 
 typedef struct rq_lobpcg_result {

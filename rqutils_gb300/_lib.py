@@ -50,7 +50,7 @@ class LobpcgParams(ctypes.Structure):
                 ('tol_dim', ctypes.c_double), ('switch_rel', ctypes.c_double),
                 ('target_rel', ctypes.c_double), ('refresh', ctypes.c_int32),
                 ('use_graph', ctypes.c_int32), ('jacobi', ctypes.c_int32),
-                ('guard', ctypes.c_int32)]
+                ('guard', ctypes.c_int32), ('restart', ctypes.c_int32), ('pad_', ctypes.c_int32)]
 
 
 class LobpcgResult(ctypes.Structure):

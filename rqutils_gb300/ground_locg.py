@@ -31,14 +31,14 @@ _VARIANTS = {'reference': L.LOBPCG_REFERENCE, 'fast': L.LOBPCG_FAST}
 
 
 def _params(D, vtype, maxiter, tol, tol_dim, variant, mixed, target_rel, switch_rel, refresh,
-            use_graph, jacobi, guard=True):
+            use_graph, jacobi, guard=True, restart=0):
     return L.LobpcgParams(maxiter=int(maxiter), variant=_VARIANTS[variant], vtype=vtype,
                           mixed=int(bool(mixed)), tol=float(tol or 0.),
                           tol_dim=float(tol_dim or 0.), switch_rel=float(switch_rel),
                           target_rel=float(target_rel or 0.), refresh=int(refresh),
                           use_graph=int(use_graph) if use_graph in (0, 1, 2) else 1,
                           jacobi=int(bool(jacobi)),
-                          guard=int(bool(guard)))
+                          guard=int(bool(guard)), restart=int(restart or 0))
 
 
 def _workspace(owner, D, prm, device):
@@ -60,13 +60,14 @@ def _info(res):
 
 def lobpcg_solve(op: DeviceOperator, x0, maxiter=1000, tol=None, tol_dim=None,
                  variant='reference', mixed=False, target_rel=None, switch_rel=1e-5, refresh=32,
-                 use_graph=True, jacobi=False, guard=True, stream=None):
+                 use_graph=True, jacobi=False, guard=True, stream=None, restart=0):
     """Run rq_lobpcg_solve on a DeviceOperator from the device vector x0 (its dtype selects the
-    value type).  Returns (eigval, x, info)."""
+    value type).  ``restart`` (FAST variant): restart the step from x every that many iterations
+    of a phase (0 = never, as the reference).  Returns (eigval, x, info)."""
     x0 = x0.contiguous()
     vt = VTYPE_OF[x0.dtype]
     prm = _params(op.D, vt, maxiter, tol, tol_dim, variant, mixed, target_rel, switch_rel,
-                  refresh, use_graph, jacobi, guard)
+                  refresh, use_graph, jacobi, guard, restart)
     ws = _workspace(op, op.D, prm, op.device)
     xout = torch.empty_like(x0)
     res = L.LobpcgResult()

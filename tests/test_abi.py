@@ -80,7 +80,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(L.Subspace) == 112
     assert ctypes.sizeof(L.Terms) == 56
     assert ctypes.sizeof(L.Operator) == 112 + 56 + 8 + 40 + 8
-    assert ctypes.sizeof(L.LobpcgParams) == 64
+    assert ctypes.sizeof(L.LobpcgParams) == 72
     assert ctypes.sizeof(L.LobpcgResult) == 48
     assert ctypes.sizeof(L.Batch) == 240
     assert L.Batch.terms.offset == 80 and L.Batch.nnz.offset == 184

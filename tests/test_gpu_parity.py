@@ -326,6 +326,37 @@ def test_persistent_loop_matches_graph_loop(cache_level, variant):
         assert abs(torch.vdot(x1, x2).item()) > 1 - 1e-10
 
 
+@pytest.mark.parametrize('use_graph', [1, 2])
+def test_fast_restart_converges_to_the_same_eigenpair(use_graph):
+    """restart = k (FAST, one problem): the step restarts from x every k iterations of a phase.
+    The solve still converges to the eigenpair of the run without restarts, with restarts from
+    nearly converged vectors (the restart projects r against x: without that, each restart near
+    convergence threw |r| back to ~1e-6 and a 10-iteration period never converged on this
+    case); iterations keep counting across restarts, and the reference variant ignores the
+    option."""
+    import torch
+    from rqutils_gb300.ground_locg import lobpcg_solve
+    case = load('n16dense')
+    prob, h, S = _problem(case, cache_level=(1, 0))
+    rng = np.random.default_rng(5)
+    x0 = torch.as_tensor(rng.normal(size=prob.sub.D)).to(prob.dtype).cuda()
+    for mixed in (False, True):
+        e0, x_0, i0 = lobpcg_solve(prob.op, x0, variant='fast', mixed=mixed, use_graph=use_graph)
+        e1, x_1, i1 = lobpcg_solve(prob.op, x0, variant='fast', mixed=mixed, use_graph=use_graph,
+                                   restart=10)
+        assert i0['converged'] and i1['converged'], (i0, i1)
+        assert abs(e1 - e0) <= 1e-10 * abs(e0)
+        assert abs(torch.vdot(x_0, x_1).item()) > 1 - 1e-8
+        if i0['niter'] > 10:
+            assert i1['niter'] != i0['niter'] or not torch.equal(x_0, x_1)
+        capped = lobpcg_solve(prob.op, x0, variant='fast', mixed=False, use_graph=use_graph,
+                              restart=3, maxiter=5)[2]
+        assert capped['niter'] == 5 and not capped['converged']
+    r0 = lobpcg_solve(prob.op, x0, variant='reference', use_graph=use_graph)
+    r1 = lobpcg_solve(prob.op, x0, variant='reference', use_graph=use_graph, restart=10)
+    assert r0[0] == r1[0] and r0[2]['niter'] == r1[2]['niter'] and torch.equal(r0[1], r1[1])
+
+
 @pytest.mark.parametrize('line', [True, False])
 @pytest.mark.parametrize('key_bits', [32, 64])
 @pytest.mark.parametrize('sectors', ['one', 'two', 'off'])
