@@ -290,8 +290,7 @@ int rq_lobpcg_solve(const rq_operator_t *op, const rq_lobpcg_params_t *prm, void
  * cudaFree, no allocating library routine, no CUDA graph) and synchronises the stream; it runs
  * with use_graph = 3 whatever prm->use_graph says: cached-connectivity and CSR operators get the
  * persistent kernel, others eager launches.  The first call on a
- * device looks up the array's device address (once per device); make that first call before any
- * stream capture.  All calls share the array and it keeps the last call's contents (the solver
+ * device looks up the array's device address (once per device).  All calls share the array and it keeps the last call's contents (the solver
  * clears what must start at zero): calls that overlap on the GPU (other streams, other threads)
  * race and must not be issued. */
 int rq_lobpcg_solve_noalloc(const rq_operator_t *op, const rq_lobpcg_params_t *prm,
