@@ -14,7 +14,8 @@ as fused CUDA kernels with FP64 reductions and device-resident scalars (``rq_lob
 Extra keyword arguments (not in the reference): ``variant`` ('reference': four matvecs per
 iteration as the reference; 'fast': one, with A x and A y carried by linearity), ``precision``
 ('fp64' or 'mixed': a 32-bit phase, then FP64 refinement), ``target_rel`` (also stop when
-|r| <= target_rel |theta|), ``jacobi`` (diagonal preconditioner), ``use_graph``.
+|r| <= target_rel |theta|), ``jacobi`` (diagonal preconditioner), ``use_graph``, ``restart``
+('fast' with a DeviceOperator: restart the step from x every that many iterations of a phase).
 """
 import ctypes
 import logging
@@ -127,7 +128,8 @@ def _is_int_scalar(v):
 
 def ground_locg(mat, xinit, args=(), maxiter=1000, tol=None, vspace=None,
                 log_level=logging.WARNING, *, variant='reference', precision=None,
-                target_rel=None, jacobi=False, use_graph=True, tol_dim=None, return_info=False):
+                target_rel=None, jacobi=False, use_graph=True, tol_dim=None, restart=0,
+                return_info=False):
     """Single-vector LOBPCG (ground_locg.py:128-157): lowest eigenvalue, eigenvector, iterations.
 
     ``xinit`` may be an integer (one-hot; with a callable ``mat`` it needs ``vspace=(dim, dtype)``,
@@ -163,7 +165,7 @@ def ground_locg(mat, xinit, args=(), maxiter=1000, tol=None, vspace=None,
     if isinstance(mat, DeviceOperator):
         eig, x, info = lobpcg_solve(mat, x0, maxiter=maxiter, tol=tol, tol_dim=tol_dim,
                                     variant=variant, mixed=mixed, target_rel=target_rel,
-                                    jacobi=jacobi, use_graph=use_graph)
+                                    jacobi=jacobi, use_graph=use_graph, restart=restart)
     else:
         if callable(mat):
             def mv(v):

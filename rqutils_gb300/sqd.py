@@ -19,7 +19,8 @@ Pipeline (all device work in librqsqd.so):
 
 Keyword-only extras: ``precision`` ('fp64' default; 'mixed' runs complex64/float32 matvecs first
 and refines in FP64), ``variant`` ('reference' | 'fast'), ``lookup`` ('hash' | 'bsearch'),
-``maxiter``, ``tol``, ``target_rel``, ``jacobi``, ``return_info``.
+``maxiter``, ``tol``, ``target_rel``, ``jacobi``, ``restart`` (FAST: restart the step from x
+every that many iterations of a phase; 0, the default, never, as the reference), ``return_info``.
 """
 import logging
 import time
@@ -176,7 +177,8 @@ class SQDProblem:
 
 def sqd(hamiltonian, states, states_size=None, return_eigvec=True, cache_level=(1, 0), *,
         precision='fp64', variant='reference', lookup='hash', maxiter=1000, tol=None,
-        target_rel=None, jacobi=False, use_graph=True, return_info=False, device=None):
+        target_rel=None, jacobi=False, use_graph=True, restart=0, return_info=False,
+        device=None):
     """Ground eigenpair of the Hamiltonian projected on the subspace spanned by ``states``.
 
     ``cache_level`` is the reference's (0, *), (1, 0|1) or (*, 2), or ``'auto'`` (not in the
@@ -199,7 +201,8 @@ def sqd(hamiltonian, states, states_size=None, return_eigvec=True, cache_level=(
     x0 = prob.initial_vector()
     eig, x, info = lobpcg_solve(prob.op, x0, maxiter=maxiter, tol=tol, tol_dim=states_size,
                                 variant=variant, mixed=(precision == 'mixed'),
-                                target_rel=target_rel, jacobi=jacobi, use_graph=use_graph)
+                                target_rel=target_rel, jacobi=jacobi, use_graph=use_graph,
+                                restart=restart)
     LOG.info('Found ground eigenpair in %f seconds.', time.time() - start)
     eigval = float(eig)
     if not return_eigvec:

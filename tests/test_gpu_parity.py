@@ -352,6 +352,12 @@ def test_fast_restart_converges_to_the_same_eigenpair(use_graph):
         capped = lobpcg_solve(prob.op, x0, variant='fast', mixed=False, use_graph=use_graph,
                               restart=3, maxiter=5)[2]
         assert capped['niter'] == 5 and not capped['converged']
+    from rqutils_gb300.sqd import sqd
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        eig = sqd(hamiltonian(case), case['states'], return_eigvec=False, variant='fast',
+                  restart=10, use_graph=use_graph)
+    assert abs(eig - float(case['eigval'])) <= 1e-9 * abs(float(case['eigval']))
     r0 = lobpcg_solve(prob.op, x0, variant='reference', use_graph=use_graph)
     r1 = lobpcg_solve(prob.op, x0, variant='reference', use_graph=use_graph, restart=10)
     assert r0[0] == r1[0] and r0[2]['niter'] == r1[2]['niter'] and torch.equal(r0[1], r1[1])
