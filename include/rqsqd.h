@@ -255,7 +255,7 @@ typedef struct rq_lobpcg_params {
                                results that would otherwise be NaN change                    */
     int32_t restart;        /* FAST, one problem: drop the search direction and restart the
                                step from x every `restart` iterations of a phase (0 = never;
-                               the reference never restarts)                                  */
+                               the reference never restarts; < 0 is rejected with RQ_E_ARG)   */
     int32_t pad_;
 } rq_lobpcg_params_t;
 

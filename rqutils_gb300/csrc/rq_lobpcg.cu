@@ -1990,6 +1990,7 @@ int solve_entry(const rq_operator_t *op, rq_matvec_fn fn, void *ctx, const rq_lo
     if (prm->maxiter < 0) return fail(RQ_E_ARG, "rq_lobpcg_solve: maxiter < 0");
     if (prm->variant != RQ_LOBPCG_REFERENCE && prm->variant != RQ_LOBPCG_FAST)
         return fail(RQ_E_ARG, "rq_lobpcg_solve: unknown variant");
+    if (prm->restart < 0) return fail(RQ_E_ARG, "rq_lobpcg_solve: restart < 0");
     const int32_t vt = prm->vtype;
     if (!fn && (vt == RQ_F32 || vt == RQ_F64) && !op->terms.is_real)
         return fail(RQ_E_ARG, "rq_lobpcg_solve: real vectors need real coefficients");
@@ -2333,6 +2334,7 @@ RQ_API int rq_batch_solve(const rq_batch_t *b, const rq_lobpcg_params_t *prm, vo
         return fail(RQ_E_ARG, "rq_batch_solve: null argument");
     if (prm->maxiter < 0 || (prm->variant != RQ_LOBPCG_REFERENCE && prm->variant != RQ_LOBPCG_FAST))
         return fail(RQ_E_ARG, "rq_batch_solve: bad maxiter or variant");
+    if (prm->restart < 0) return fail(RQ_E_ARG, "rq_batch_solve: restart < 0");
     const int32_t vt = prm->vtype;
     if ((vt == RQ_F32 || vt == RQ_F64) && !b->terms.is_real)
         return fail(RQ_E_ARG, "rq_batch_solve: real vectors need real coefficients");

@@ -75,6 +75,24 @@ def test_host_only_entry_points(libpath):
     assert lib.rq_line_filter_bits(1 << 20, 11, ctypes.byref(lb)) == L.E_ARG
 
 
+def test_lobpcg_parameters_validated_on_the_host(libpath):
+    """rq_lobpcg_solve rejects a negative restart period (and a negative maxiter) before it
+    touches the device."""
+    from rqutils_gb300 import _lib as L
+    lib = L.lib()
+    op = L.Operator()
+    op.sub.D = 16
+    res = L.LobpcgResult()
+    dummy = ctypes.c_void_p(16)  # never dereferenced: validation fails first
+    prm = L.LobpcgParams(maxiter=10, variant=L.LOBPCG_FAST, vtype=L.C128, restart=-1)
+    assert lib.rq_lobpcg_solve(ctypes.byref(op), ctypes.byref(prm), dummy, dummy, dummy,
+                               ctypes.byref(res), None) == L.E_ARG
+    assert b'restart' in lib.rq_last_error()
+    prm = L.LobpcgParams(maxiter=-1, variant=L.LOBPCG_FAST, vtype=L.C128)
+    assert lib.rq_lobpcg_solve(ctypes.byref(op), ctypes.byref(prm), dummy, dummy, dummy,
+                               ctypes.byref(res), None) == L.E_ARG
+
+
 def test_struct_layouts():
     from rqutils_gb300 import _lib as L
     assert ctypes.sizeof(L.Subspace) == 112
